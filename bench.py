@@ -1,0 +1,310 @@
+#!/usr/bin/env python3
+"""Benchmark of the GravHopper force-and-integrate path on GB300.
+
+Default workload: one drift-kick-drift leapfrog step of an equal-mass Plummer sphere
+with N = 1,048,576 particles (b = 1 pc, M = 1e6 Msun, eps = 0.05 pc, dt = 0.005 Myr),
+direct-sum force in the mixed form (FP32 pair arithmetic, compensated accumulation,
+FP64 state), one fused kernel launch per step.  A step is N*(N-1) pair interactions;
+``value`` is pair interactions per second in Gpair/s with the state resident in HBM,
+the L2 cache flushed before every timed step.
+
+Also reported on the same line:
+* ``e2e``: the same force through the reference-facing C-ABI call with host buffers
+  (``gh_direct_host``: pinned host -> device copy, force, device -> host copy),
+* ``roofline``: the mixed kernel against the FP32 FMA-pipe peak measured live
+  (12 FMA-pipe lane-ops per pair),
+* ``secondary``: the FP64 form's Gpair/s (N = 65,536), the mixed form's error against
+  the FP64 form on sampled targets, the mixed/FP64 throughput ratio,
+* ``cpu_baseline``: the CPU oracle (a restatement of the reference's C loops) on the
+  host cores, on a bounded sample of targets.
+
+``--impl reference`` times that CPU implementation alone on the same metric.
+Under torchrun with N > 1, every rank runs its own system (replicas; weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Direct-sum Gpair/s & tree particle-steps/s, mixed vs FP64, 1 GB300 @ <=1e-6 err"
+UNIT = "Gpair/s"
+PAIR_OPS = 12  # FP32 FMA-pipe lane-ops per pair: 3 sub, 3 fma, 3 mul, 3 fma
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=1 << 20)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--cpu-targets", type=int, default=4096,
+                    help="targets in the CPU-baseline sample (each against all N sources)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms in the background."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.rows = []
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "200", "-i", str(self.gpu)],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                self.rows.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in self.rows for i in range(4) if r[5 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows),
+                "power_w_max": max((float(r[3]) for r in self.rows
+                                    if r[3].replace(".", "").isdigit()), default=None)}
+
+
+def cpu_baseline(n, targets, seed=0):
+    """Oracle direct sum (the reference's loop order, FP64) on a sample of targets."""
+    import numpy as np
+
+    from gravhopper_gb300 import ics
+    from oracle import oracle
+    ic = ics.plummer(n, seed=seed)
+    rng = np.random.default_rng(1)
+    idx = rng.choice(n, size=min(targets, n), replace=False)
+    threads = oracle.default_threads()
+    oracle.direct_summation_position(ic["pos"], ic["mass"], ic["pos"][idx[:64]], 5e-5, nthreads=threads)
+    t0 = time.perf_counter()
+    oracle.direct_summation_position(ic["pos"], ic["mass"], ic["pos"][idx], 5e-5, nthreads=threads)
+    dt = time.perf_counter() - t0
+    pairs = float(len(idx)) * n
+    return {"value": pairs / dt / 1e9, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{len(idx)} targets x {n} sources (FP64, reference loop order), {dt:.2f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    res = []
+    for k in range(args.warmup + args.steps):
+        r = cpu_baseline(args.n, max(64, args.cpu_targets // 2), seed=k)
+        if k >= args.warmup:
+            res.append(r)
+    val = statistics.median(r["value"] for r in res)
+    line = {"impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": float(args.n) * (args.n - 1) / (val * 1e9) * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": _config(args),
+            "cpu_baseline": {"value": val, "unit": UNIT, "cores": res[0]["cores"], "kind": "port",
+                             "sample": res[0]["sample"] + " per step; ms_per_step extrapolates to N*(N-1)"},
+            "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def _config(args):
+    return {"workload": f"direct-sum DKD leapfrog step, Plummer sphere N={args.n} (b=1 pc, M=1e6 Msun, "
+                        f"eps=0.05 pc, dt=0.005 Myr)",
+            "precision": args.precision, "n": args.n, "pairs_per_step": args.n * (args.n - 1),
+            "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"}
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import _capi, engine, ics
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    _capi.load()
+    n = args.n
+    ic = ics.plummer(n, seed=rank)
+    x = torch.from_numpy(ic["pos"]).to(dev)
+    v = torch.from_numpy(ic["vel"]).to(dev)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    eps, dt = 5e-5, 0.005
+    stream = torch.cuda.current_stream()
+    fp32_peak, fp64_peak = _capi.measure_fma_peaks()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def step():
+        engine.run_dkd(x, v, m, 1, dt, eps, algorithm="direct", precision=args.precision)
+
+    for _ in range(args.warmup):
+        step()
+    barrier()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    _capi.kernel_timing_collect()
+    _capi.kernel_timing(True)
+    launches0 = _capi.launch_count()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.zero_()
+            ev[k][0].record(stream)
+            step()
+            ev[k][1].record(stream)
+        barrier()
+    launches = _capi.launch_count() - launches0
+    _capi.kernel_timing(False)
+    kern_ms, kern_n = _capi.kernel_timing_collect()
+    step_ms = sum(a.elapsed_time(b) for a, b in ev)
+    t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    step_ms_max = float(t.item())
+    pairs = float(n) * (n - 1)
+    value = world * pairs * args.steps / (step_ms_max * 1e-3) / 1e9
+
+    # End to end through the host-buffer C ABI (pinned host memory, copies timed).
+    hp = torch.from_numpy(ic["pos"]).pin_memory()
+    hm = torch.from_numpy(ic["mass"]).pin_memory()
+    ho = torch.empty((n, 3), dtype=torch.float64).pin_memory()
+    prec = _capi.PRECISIONS[args.precision]
+    e2e_steps = max(1, min(args.steps, 5))
+    _capi.call("gh_direct_host", hp.data_ptr(), hm.data_ptr(), n, None, 0, eps, prec, ho.data_ptr())
+    barrier()
+    e2e_s = 0.0
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        _capi.call("gh_direct_host", hp.data_ptr(), hm.data_ptr(), n, None, 0, eps, prec, ho.data_ptr())
+        e2e_s += time.perf_counter() - t0
+    e2e = {"value": world * pairs * e2e_steps / e2e_s / 1e9, "unit": UNIT,
+           "h2d_bytes_per_step": n * 3 * 8 + n * 8, "d2h_bytes_per_step": n * 3 * 8}
+
+    kern_avg_s = kern_ms / max(kern_n, 1) * 1e-3
+    achieved = pairs / kern_avg_s / 1e9
+    peak = fp32_peak / PAIR_OPS / 1e9
+    roofline = {"bound": "fp32", "kernel": "direct_mixed_kernel" if args.precision == "mixed" else
+                "direct_f64_kernel", "achieved": achieved, "peak": peak, "unit": UNIT,
+                "frac": achieved / peak, "traffic": None,
+                "peak_source": f"measured live: f32x2 FMA chains, {fp32_peak / 1e12:.1f} T lane-op/s "
+                               f"/ {PAIR_OPS} lane-ops per pair",
+                "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
+
+    secondary = {}
+    if not args.no_secondary:
+        secondary = measure_secondary(ic, dev, fp64_peak, achieved if args.precision == "mixed" else None)
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": step_ms_max / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None,
+                "dtype": "f32" if args.precision == "mixed" else "f64",
+                "data": "synthetic", "config": _config(args), "roofline": roofline,
+                "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
+                "secondary": secondary}
+        line["cpu_baseline"] = cpu_baseline(n, args.cpu_targets)
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def measure_secondary(ic, dev, fp64_peak, mixed_gpair):
+    """FP64-form throughput and mixed-form accuracy on this GPU."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import _capi, engine, ics
+    out = {}
+    # FP64 form throughput at N = 65,536 (one force evaluation, kernel-timed).
+    s = ics.plummer(65536, seed=7)
+    xs = torch.from_numpy(s["pos"]).to(dev)
+    ms_ = torch.from_numpy(s["mass"]).to(dev)
+    engine.direct_force(xs, ms_, 5e-5, precision="fp64")
+    torch.cuda.synchronize()
+    _capi.kernel_timing_collect()
+    _capi.kernel_timing(True)
+    engine.direct_force(xs, ms_, 5e-5, precision="fp64")
+    _capi.kernel_timing(False)
+    kms, _ = _capi.kernel_timing_collect()
+    g64 = 65536.0 * 65535 / (kms * 1e-3) / 1e9
+    out["fp64_n"] = 65536
+    out["fp64_gpair_s"] = g64
+    out["fp64_lane_ops_peak_t"] = fp64_peak / 1e12
+    if mixed_gpair:
+        out["mixed_over_fp64"] = mixed_gpair / g64
+    # Mixed-form error against the FP64 form (bit-identical to the oracle) on 4096
+    # sampled targets of the N = 1,048,576 system.
+    n = ic["pos"].shape[0]
+    rng = np.random.default_rng(2)
+    idx = torch.from_numpy(rng.choice(n, size=min(4096, n), replace=False)).to(dev)
+    x = torch.from_numpy(ic["pos"]).to(dev)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    a_mixed = engine.direct_force(x, m, 5e-5, precision="mixed")[idx]
+    a64 = engine.direct_force(x, m, 5e-5, force_pos=x[idx].contiguous(), precision="fp64")
+    err = torch.linalg.norm(a_mixed - a64, dim=1) / torch.linalg.norm(a64, dim=1)
+    out["mixed_rel_err_rms"] = float(torch.sqrt(torch.mean(err * err)))
+    out["mixed_rel_err_max"] = float(err.max())
+    out["mixed_err_sample"] = f"{idx.numel()} targets of N={n} vs FP64 form"
+    return out
+
+
+if __name__ == "__main__":
+    main()

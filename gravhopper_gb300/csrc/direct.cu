@@ -1,0 +1,291 @@
+// Direct-sum force calls and the on-device leapfrog run loop.
+#include <mutex>
+
+#include "direct.cuh"
+#include "engine.h"
+
+namespace gh {
+
+static_assert(MX_JT == MX_THREADS, "one source per thread per chunk fill");
+
+// ---------------------------------------------------------------------------
+// Small kernels: mass-weighted centre (deterministic two-pass), conversion to
+// FP32 relative coordinates, first half-drift of a run.
+// ---------------------------------------------------------------------------
+constexpr int COM_THREADS = 256;
+constexpr int COM_MAX_BLOCKS = 512;
+
+__global__ void com_partial_kernel(const double* __restrict__ pos, const double* __restrict__ mass,
+                                   int64_t n, dvec4* __restrict__ part) {
+  __shared__ dvec4 red[COM_THREADS];
+  const int64_t per = (n + gridDim.x - 1) / gridDim.x;
+  const int64_t b0 = (int64_t)blockIdx.x * per;
+  const int64_t b1 = b0 + per < n ? b0 + per : n;
+  dvec4 acc = make_dvec4(0.0, 0.0, 0.0, 0.0);
+  for (int64_t i = b0 + threadIdx.x; i < b1; i += COM_THREADS) {
+    double m = mass[i];
+    acc.x += m * pos[3 * i];
+    acc.y += m * pos[3 * i + 1];
+    acc.z += m * pos[3 * i + 2];
+    acc.w += m;
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = COM_THREADS / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+      dvec4 o = red[threadIdx.x + s];
+      red[threadIdx.x].x += o.x;
+      red[threadIdx.x].y += o.y;
+      red[threadIdx.x].z += o.z;
+      red[threadIdx.x].w += o.w;
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = red[0];
+}
+
+__global__ void com_final_kernel(const dvec4* __restrict__ part, int nb, double* __restrict__ origin) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  dvec4 s = make_dvec4(0.0, 0.0, 0.0, 0.0);
+  for (int b = 0; b < nb; b++) {
+    s.x += part[b].x;
+    s.y += part[b].y;
+    s.z += part[b].z;
+    s.w += part[b].w;
+  }
+  if (s.w != 0.0 && isfinite(s.x / s.w) && isfinite(s.y / s.w) && isfinite(s.z / s.w)) {
+    origin[0] = s.x / s.w;
+    origin[1] = s.y / s.w;
+    origin[2] = s.z / s.w;
+  } else {
+    origin[0] = origin[1] = origin[2] = 0.0;
+  }
+}
+
+__global__ void to_f32_kernel(const double* __restrict__ pos, const double* __restrict__ mass,
+                              int64_t n, const double* __restrict__ origin, float4* __restrict__ out) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double o0 = origin[0], o1 = origin[1], o2 = origin[2];
+  out[i] = make_float4((float)dsub(pos[3 * i], o0), (float)dsub(pos[3 * i + 1], o1),
+                       (float)dsub(pos[3 * i + 2], o2), mass ? (float)mass[i] : 0.f);
+}
+
+__global__ void drift_prepare_kernel(const double* __restrict__ x, const double* __restrict__ v,
+                                     const double* __restrict__ mass, int64_t n, double dt,
+                                     const double* __restrict__ origin, float4* __restrict__ src,
+                                     double* __restrict__ xh) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double h[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) h[k] = drift_half(x[3 * i + k], v[3 * i + k], dt);
+  if (src)
+    src[i] = make_float4((float)dsub(h[0], origin[0]), (float)dsub(h[1], origin[1]),
+                         (float)dsub(h[2], origin[2]), (float)mass[i]);
+  if (xh) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) xh[3 * i + k] = h[k];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Workspace for the direct path (one per device).
+// ---------------------------------------------------------------------------
+struct DirectWS {
+  Buffer src[2], tgt, xh[2], partials, counters, origin, com_part;
+  size_t counters_zeroed = 0;
+};
+static DirectWS g_ws[64];
+static std::recursive_mutex g_mu;
+
+static int mixed_grid_cap(int num_sms, bool guard) {
+  static int occ[2] = {0, 0};
+  int& o = occ[guard ? 1 : 0];
+  if (o == 0) {
+    cudaError_t e;
+    if (guard)
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<true, EpiStore>,
+                                                        MX_THREADS, 0);
+    else
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<false, EpiStore>,
+                                                        MX_THREADS, 0);
+    if (e != cudaSuccess || o < 1) o = 1;
+  }
+  return o * num_sms;
+}
+
+StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap) {
+  StreamK s;
+  s.n_tiles = (nt + MX_TILE - 1) / MX_TILE;
+  s.chunks = (np + MX_JT - 1) / MX_JT;
+  s.units = s.n_tiles * s.chunks;
+  s.grid = s.units < grid_cap ? s.units : grid_cap;
+  if (s.grid < 1) s.grid = 1;
+  return s;
+}
+
+// Mass-weighted centre of (pos, mass) into ws.origin (3 doubles).
+static int compute_origin(DirectWS& ws, const double* pos, const double* mass, int64_t n,
+                          cudaStream_t st) {
+  GH_TRY(ensure(ws.origin, 4 * sizeof(double)));
+  GH_TRY(ensure(ws.com_part, COM_MAX_BLOCKS * sizeof(dvec4)));
+  int nb = (int)((n + 4 * COM_THREADS - 1) / (4 * COM_THREADS));
+  if (nb < 1) nb = 1;
+  if (nb > COM_MAX_BLOCKS) nb = COM_MAX_BLOCKS;
+  com_partial_kernel<<<nb, COM_THREADS, 0, st>>>(pos, mass, n, (dvec4*)ws.com_part.ptr);
+  GH_LAUNCH_CHECK();
+  com_final_kernel<<<1, 32, 0, st>>>((const dvec4*)ws.com_part.ptr, nb, (double*)ws.origin.ptr);
+  GH_LAUNCH_CHECK();
+  return GH_OK;
+}
+
+static int ensure_streamk(DirectWS& ws, const StreamK& sk, cudaStream_t st) {
+  GH_TRY(ensure(ws.partials, (size_t)(2 * sk.grid * MX_SLOT_FLOATS) * sizeof(float)));
+  size_t cbytes = (size_t)sk.n_tiles * sizeof(int);
+  if (ws.counters.bytes < cbytes || ws.counters_zeroed < cbytes) {
+    GH_TRY(ensure(ws.counters, cbytes));
+    GH_CUDA_TRY(cudaMemsetAsync(ws.counters.ptr, 0, ws.counters.bytes, st));
+    ws.counters_zeroed = ws.counters.bytes;
+  }
+  return GH_OK;
+}
+
+template <class Epi>
+static int launch_mixed(DirectWS& ws, const float4* src, int64_t np, const float4* tgt, int64_t nt,
+                        double eps, const Epi& epi, cudaStream_t st) {
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  const float eps2 = (float)(eps * eps);
+  const bool guard = !(eps2 > 0.f);
+  StreamK sk = mixed_plan(np, nt, mixed_grid_cap(di.num_sms, guard));
+  if (sk.units == 0) return GH_OK;
+  GH_TRY(ensure_streamk(ws, sk, st));
+  prof_begin(st);
+  if (guard)
+    direct_mixed_kernel<true, Epi><<<(unsigned)sk.grid, MX_THREADS, 0, st>>>(
+        src, np, tgt, nt, eps2, sk, (float*)ws.partials.ptr, (int*)ws.counters.ptr, epi);
+  else
+    direct_mixed_kernel<false, Epi><<<(unsigned)sk.grid, MX_THREADS, 0, st>>>(
+        src, np, tgt, nt, eps2, sk, (float*)ws.partials.ptr, (int*)ws.counters.ptr, epi);
+  prof_end(st);
+  GH_LAUNCH_CHECK();
+  return GH_OK;
+}
+
+template <bool SELF, class Epi>
+static int launch_f64(const double* spos, const double* smass, int64_t np, const double* tpos,
+                      int64_t nt, double eps, const Epi& epi, cudaStream_t st) {
+  const int64_t per = F64_THREADS * F64_R;
+  const int64_t blocks = (nt + per - 1) / per;
+  if (blocks == 0) return GH_OK;
+  prof_begin(st);
+  direct_f64_kernel<SELF, Epi><<<(unsigned)blocks, F64_THREADS, 0, st>>>(spos, smass, np, tpos, nt,
+                                                                         eps * eps, epi);
+  prof_end(st);
+  GH_LAUNCH_CHECK();
+  return GH_OK;
+}
+
+static int check_common(int64_t np, int64_t nt, double eps, int precision) {
+  if (np < 0 || nt < 0) return set_error(GH_ERR_ARG, "negative particle count (np=%lld, nf=%lld)",
+                                         (long long)np, (long long)nt);
+  if (precision != GH_PREC_FP64 && precision != GH_PREC_MIXED)
+    return set_error(GH_ERR_ARG, "unknown precision %d", precision);
+  if (!(eps >= 0.0) || eps != eps) return set_error(GH_ERR_ARG, "eps must be >= 0 (got %g)", eps);
+  return GH_OK;
+}
+
+int direct_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt,
+                 double eps, int precision, double* acc, cudaStream_t st) {
+  GH_TRY(check_common(np, nt, eps, precision));
+  const bool self = (tpos == nullptr);
+  if (self) nt = np;
+  if (nt == 0) return GH_OK;
+  if (!acc || (np > 0 && (!pos || !mass)))
+    return set_error(GH_ERR_ARG, "null buffer passed to direct force");
+  if (np == 0) {
+    GH_CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)nt * 3 * sizeof(double), st));
+    return GH_OK;
+  }
+  EpiStore epi{acc};
+  if (precision == GH_PREC_FP64) {
+    if (self) return launch_f64<true>(pos, mass, np, pos, np, eps, epi, st);
+    return launch_f64<false>(pos, mass, np, tpos, nt, eps, epi, st);
+  }
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  DirectWS& ws = g_ws[di.device];
+  GH_TRY(compute_origin(ws, pos, mass, np, st));
+  GH_TRY(ensure(ws.src[0], (size_t)np * sizeof(float4)));
+  const int T = 256;
+  to_f32_kernel<<<(unsigned)((np + T - 1) / T), T, 0, st>>>(pos, mass, np, (const double*)ws.origin.ptr,
+                                                           (float4*)ws.src[0].ptr);
+  GH_LAUNCH_CHECK();
+  const float4* tgt = (const float4*)ws.src[0].ptr;
+  if (!self) {
+    GH_TRY(ensure(ws.tgt, (size_t)nt * sizeof(float4)));
+    to_f32_kernel<<<(unsigned)((nt + T - 1) / T), T, 0, st>>>(tpos, nullptr, nt,
+                                                             (const double*)ws.origin.ptr,
+                                                             (float4*)ws.tgt.ptr);
+    GH_LAUNCH_CHECK();
+    tgt = (const float4*)ws.tgt.ptr;
+  }
+  return launch_mixed(ws, (const float4*)ws.src[0].ptr, np, tgt, nt, eps, epi, st);
+}
+
+int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
+               double eps, int precision, double* hist_x, double* hist_v, int64_t stride,
+               cudaStream_t st) {
+  std::lock_guard<std::recursive_mutex> lk(g_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  DirectWS& ws = g_ws[di.device];
+  const int T = 256;
+  const unsigned nb = (unsigned)((np + T - 1) / T);
+  if (precision == GH_PREC_MIXED) {
+    GH_TRY(compute_origin(ws, x, mass, np, st));
+    GH_TRY(ensure(ws.src[0], (size_t)np * sizeof(float4)));
+    GH_TRY(ensure(ws.src[1], (size_t)np * sizeof(float4)));
+    drift_prepare_kernel<<<nb, T, 0, st>>>(x, v, mass, np, dt, (const double*)ws.origin.ptr,
+                                           (float4*)ws.src[0].ptr, nullptr);
+    GH_LAUNCH_CHECK();
+  } else {
+    GH_TRY(ensure(ws.xh[0], (size_t)np * 3 * sizeof(double)));
+    GH_TRY(ensure(ws.xh[1], (size_t)np * 3 * sizeof(double)));
+    drift_prepare_kernel<<<nb, T, 0, st>>>(x, v, mass, np, dt, nullptr, nullptr,
+                                           (double*)ws.xh[0].ptr);
+    GH_LAUNCH_CHECK();
+  }
+  for (int64_t s = 0; s < nsteps; s++) {
+    const int cur = (int)(s & 1), nxt = cur ^ 1;
+    EpiDKD epi;
+    epi.x = x;
+    epi.v = v;
+    epi.mass = mass;
+    epi.dt = dt;
+    epi.hist_x = epi.hist_v = nullptr;
+    if (hist_x && stride > 0 && (s + 1) % stride == 0) {
+      const int64_t slot = (s + 1) / stride - 1;
+      epi.hist_x = hist_x + slot * np * 3;
+      epi.hist_v = hist_v + slot * np * 3;
+    }
+    if (precision == GH_PREC_MIXED) {
+      epi.src_next = (float4*)ws.src[nxt].ptr;
+      epi.xh_next = nullptr;
+      epi.origin = (const double*)ws.origin.ptr;
+      const float4* src = (const float4*)ws.src[cur].ptr;
+      GH_TRY(launch_mixed(ws, src, np, src, np, eps, epi, st));
+    } else {
+      epi.src_next = nullptr;
+      epi.xh_next = (double*)ws.xh[nxt].ptr;
+      epi.origin = nullptr;
+      const double* xh = (const double*)ws.xh[cur].ptr;
+      GH_TRY(launch_f64<true>(xh, mass, np, xh, np, eps, epi, st));
+    }
+  }
+  return GH_OK;
+}
+
+}  // namespace gh

@@ -1,0 +1,403 @@
+// Direct-sum force kernels and the leapfrog epilogues they can run in place of a
+// plain store.  Included by direct.cu (force calls, run loop) and by the no-alloc
+// variant; everything here is header-only device code plus launch helpers.
+#pragma once
+
+#include "gh_common.cuh"
+
+namespace gh {
+
+// ---------------------------------------------------------------------------
+// Packed FP32 pairs (Blackwell f32x2 ALU ops): one instruction, two lanes of work.
+// ---------------------------------------------------------------------------
+typedef unsigned long long f2;
+
+__device__ __forceinline__ f2 f2make(float a, float b) {
+  f2 r;
+  asm("mov.b64 %0, {%1,%2};" : "=l"(r) : "f"(a), "f"(b));
+  return r;
+}
+__device__ __forceinline__ void f2split(f2 v, float& a, float& b) {
+  asm("mov.b64 {%0,%1}, %2;" : "=f"(a), "=f"(b) : "l"(v));
+}
+__device__ __forceinline__ f2 f2add(f2 a, f2 b) {
+  f2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2sub(f2 a, f2 b) {
+  f2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2mul(f2 a, f2 b) {
+  f2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f2 f2fma(f2 a, f2 b, f2 c) {
+  f2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+// Two-sum on both lanes: (s, e) with s + e == a + b exactly, per lane.
+__device__ __forceinline__ void f2two_sum(f2 a, f2 b, f2& s, f2& e) {
+  s = f2add(a, b);
+  f2 bb = f2sub(s, a);
+  e = f2add(f2sub(a, f2sub(s, bb)), f2sub(b, bb));
+}
+
+// ---------------------------------------------------------------------------
+// Leapfrog (drift-kick-drift) arithmetic of Simulation.perform_timestep,
+// gravhopper/gravhopper.py:405-416, in kpc, km/s, Myr, with no FMA contraction:
+//   xh = x + ((0.5*v)*dt)*F          (F = km*Myr/s -> kpc)
+//   v' = v + (a*ACC)*dt              (ACC = G*Msun/kpc^2 in km/s/Myr)
+//   x' = xh + ((0.5*v')*dt)*F
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double drift_half(double x, double v, double dt) {
+  return dadd(x, dmul(dmul(dmul(0.5, v), dt), GH_KMS_MYR_TO_KPC));
+}
+__device__ __forceinline__ double kick(double v, double a_code, double dt) {
+  return dadd(v, dmul(dmul(a_code, GH_ACCEL_UNIT), dt));
+}
+
+// ---------------------------------------------------------------------------
+// Epilogues.  Each is called once per target with the code-unit acceleration.
+// ---------------------------------------------------------------------------
+
+// Store the acceleration (code units) into acc[(N,3)].
+struct EpiStore {
+  double* acc;
+  __device__ __forceinline__ void operator()(int64_t i, double ax, double ay, double az) const {
+    acc[3 * i + 0] = ax;
+    acc[3 * i + 1] = ay;
+    acc[3 * i + 2] = az;
+  }
+};
+
+// Finish a DKD step for particle i and prepare the next step's sources.
+//   x, v     : state at the start of the step (read), state after it (written)
+//   src_next : next step's half-drifted sources; float4 relative to `origin` for the
+//              mixed form, or FP64 (N,3) in `xh_next` for the FP64 form
+//   hist_x/v : optional snapshot slots (N,3) written with the new state
+struct EpiDKD {
+  double* x;
+  double* v;
+  const double* mass;
+  float4* src_next;      // mixed form (may be null)
+  double* xh_next;       // FP64 form (may be null)
+  double* hist_x;
+  double* hist_v;
+  const double* origin;  // device pointer to 3 doubles (mixed form)
+  double dt;
+  __device__ __forceinline__ void operator()(int64_t i, double ax, double ay, double az) const {
+    double a[3] = {ax, ay, az};
+    double xn[3], vn[3], xh2[3];
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      double x0 = x[3 * i + k], v0 = v[3 * i + k];
+      double xh = drift_half(x0, v0, dt);
+      double v1 = kick(v0, a[k], dt);
+      double x1 = drift_half(xh, v1, dt);
+      xn[k] = x1;
+      vn[k] = v1;
+      xh2[k] = drift_half(x1, v1, dt);
+    }
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      x[3 * i + k] = xn[k];
+      v[3 * i + k] = vn[k];
+    }
+    if (hist_x) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        hist_x[3 * i + k] = xn[k];
+        hist_v[3 * i + k] = vn[k];
+      }
+    }
+    if (src_next) {
+      src_next[i] = make_float4((float)dsub(xh2[0], origin[0]), (float)dsub(xh2[1], origin[1]),
+                                (float)dsub(xh2[2], origin[2]), (float)mass[i]);
+    }
+    if (xh_next) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) xh_next[3 * i + k] = xh2[k];
+    }
+  }
+};
+
+// ---------------------------------------------------------------------------
+// FP64 form: bit-exact restatement of directsummation_workhorse
+// (gravhopper/_jbgrav.c:140-193) and directsummation_position_workhorse
+// (:299-353).  One thread owns F64_R targets and walks every source in ascending
+// order, so each component is summed in exactly the reference's order.
+// ---------------------------------------------------------------------------
+constexpr int F64_THREADS = 128;
+constexpr int F64_R = 2;
+constexpr int F64_JT = 128;
+
+template <bool SELF, class Epi>
+__global__ void __launch_bounds__(F64_THREADS)
+    direct_f64_kernel(const double* __restrict__ spos, const double* __restrict__ smass, int64_t np,
+                      const double* __restrict__ tpos, int64_t nt, double eps2, Epi epi) {
+  __shared__ dvec4 tile[F64_JT];
+  const int64_t base = (int64_t)blockIdx.x * (F64_THREADS * F64_R) + threadIdx.x;
+  double tx[F64_R], ty[F64_R], tz[F64_R], ax[F64_R], ay[F64_R], az[F64_R];
+  int64_t ti[F64_R];
+#pragma unroll
+  for (int r = 0; r < F64_R; r++) {
+    ti[r] = base + r * F64_THREADS;
+    int64_t t = ti[r] < nt ? ti[r] : 0;
+    tx[r] = nt ? tpos[3 * t + 0] : 0.0;
+    ty[r] = nt ? tpos[3 * t + 1] : 0.0;
+    tz[r] = nt ? tpos[3 * t + 2] : 0.0;
+    ax[r] = ay[r] = az[r] = 0.0;
+  }
+  for (int64_t j0 = 0; j0 < np; j0 += F64_JT) {
+    __syncthreads();
+    for (int k = threadIdx.x; k < F64_JT; k += F64_THREADS) {
+      int64_t j = j0 + k;
+      if (j < np) tile[k] = make_dvec4(spos[3 * j], spos[3 * j + 1], spos[3 * j + 2], smass[j]);
+    }
+    __syncthreads();
+    const int jn = (np - j0) < F64_JT ? (int)(np - j0) : F64_JT;
+    for (int k = 0; k < jn; k++) {
+      const dvec4 s = tile[k];
+#pragma unroll
+      for (int r = 0; r < F64_R; r++) {
+        if (SELF && (j0 + k) == ti[r]) continue;
+        double dx = dsub(s.x, tx[r]);
+        double dy = dsub(s.y, ty[r]);
+        double dz = dsub(s.z, tz[r]);
+        double r2 = dmul(dx, dx);
+        r2 = dadd(r2, dmul(dy, dy));
+        r2 = dadd(r2, dmul(dz, dz));
+        double ss = dadd(r2, eps2);
+        double inv = ddiv(ddiv(1.0, ss), dsqrt(ss));
+        if (!SELF && ss == 0.0) inv = 0.0;
+        ax[r] = dadd(ax[r], dmul(dmul(s.w, dx), inv));
+        ay[r] = dadd(ay[r], dmul(dmul(s.w, dy), inv));
+        az[r] = dadd(az[r], dmul(dmul(s.w, dz), inv));
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < F64_R; r++)
+    if (ti[r] < nt) epi(ti[r], ax[r], ay[r], az[r]);
+}
+
+// ---------------------------------------------------------------------------
+// Mixed form: FP32 pair arithmetic on coordinates relative to an origin, f32x2
+// packed over pairs of targets, per-chunk FP32 partial sums folded into a
+// (hi, lo) two-sum accumulator per target and component, FP64 epilogue.
+//
+// Work split ("stream-K"): the (target tile, source chunk) grid of
+// n_tiles x chunks units is cut into `grid` equal contiguous ranges, one per
+// persistent CTA.  A tile split across CTAs leaves per-CTA partials in scratch;
+// the CTA that finishes last (per-tile counter) combines them in CTA order, so
+// the result does not depend on timing, and runs the epilogue.
+// ---------------------------------------------------------------------------
+constexpr int MX_THREADS = 256;
+constexpr int MX_P = 2;                      // f32x2 packs per thread
+constexpr int MX_R = 2 * MX_P;               // targets per thread
+constexpr int MX_TILE = MX_THREADS * MX_R;   // targets per tile
+constexpr int MX_JT = 256;                   // sources per shared-memory chunk
+
+struct StreamK {
+  int64_t n_tiles;
+  int64_t chunks;
+  int64_t units;
+  int64_t grid;
+};
+
+__host__ __device__ __forceinline__ int64_t sk_start(const StreamK& s, int64_t g) {
+  return (g * s.units) / s.grid;
+}
+// CTA whose range contains unit u.
+__host__ __device__ __forceinline__ int64_t sk_owner(const StreamK& s, int64_t u) {
+  return ((u + 1) * s.grid + s.units - 1) / s.units - 1;
+}
+
+// Per-CTA scratch for split tiles: 2 slots (first and last tile of its range),
+// each 6 floats (hi/lo for x, y, z) per target.
+constexpr int64_t MX_SLOT_FLOATS = (int64_t)6 * MX_TILE;
+
+template <bool GUARD, class Epi>
+__global__ void __launch_bounds__(MX_THREADS, 2)
+    direct_mixed_kernel(const float4* __restrict__ src, int64_t np, const float4* __restrict__ tgt,
+                        int64_t nt, float eps2, StreamK sk, float* __restrict__ partials,
+                        int* __restrict__ counters, Epi epi) {
+  // Sources duplicated per lane pair: (x,x,y,y) and (z,z,m,m).
+  __shared__ __align__(16) float4 tile[2 * MX_JT];
+  __shared__ int s_last;
+  const int tid = threadIdx.x;
+  const int64_t g = blockIdx.x;
+  const int64_t u_begin = sk_start(sk, g), u_end = sk_start(sk, g + 1);
+  const f2 E2 = f2make(eps2, eps2);
+
+  int64_t u = u_begin;
+  while (u < u_end) {
+    const int64_t t = u / sk.chunks;
+    const int64_t c0 = u - t * sk.chunks;
+    const int64_t c1 = (sk.chunks - c0) < (u_end - u) ? sk.chunks : c0 + (u_end - u);
+    u += c1 - c0;
+
+    // Targets of tile t: target r of this thread is t*TILE + r*THREADS + tid.
+    f2 tx[MX_P], ty[MX_P], tz[MX_P];
+    f2 hx[MX_P], hy[MX_P], hz[MX_P], lx[MX_P], ly[MX_P], lz[MX_P];
+#pragma unroll
+    for (int p = 0; p < MX_P; p++) {
+      float4 q[2];
+#pragma unroll
+      for (int h = 0; h < 2; h++) {
+        int64_t i = t * MX_TILE + (2 * p + h) * MX_THREADS + tid;
+        q[h] = i < nt ? tgt[i] : make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+      tx[p] = f2make(q[0].x, q[1].x);
+      ty[p] = f2make(q[0].y, q[1].y);
+      tz[p] = f2make(q[0].z, q[1].z);
+      hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = 0ull;
+    }
+
+    for (int64_t c = c0; c < c1; c++) {
+      __syncthreads();
+      {
+        const int64_t j = c * MX_JT + tid;
+        // Padding sources have zero mass at the origin: their terms are exactly 0.
+        float4 s = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        tile[2 * tid + 0] = make_float4(s.x, s.x, s.y, s.y);
+        tile[2 * tid + 1] = make_float4(s.z, s.z, s.w, s.w);
+      }
+      __syncthreads();
+      f2 px[MX_P], py[MX_P], pz[MX_P];
+#pragma unroll
+      for (int p = 0; p < MX_P; p++) px[p] = py[p] = pz[p] = 0ull;
+#pragma unroll 4
+      for (int k = 0; k < MX_JT; k++) {
+        const float4 a = tile[2 * k + 0];
+        const float4 b = tile[2 * k + 1];
+        const f2 X = f2make(a.x, a.y), Y = f2make(a.z, a.w);
+        const f2 Z = f2make(b.x, b.y), M = f2make(b.z, b.w);
+#pragma unroll
+        for (int p = 0; p < MX_P; p++) {
+          f2 dx = f2sub(X, tx[p]);
+          f2 dy = f2sub(Y, ty[p]);
+          f2 dz = f2sub(Z, tz[p]);
+          f2 r2 = f2fma(dx, dx, E2);
+          r2 = f2fma(dy, dy, r2);
+          r2 = f2fma(dz, dz, r2);
+          float r2a, r2b;
+          f2split(r2, r2a, r2b);
+          float ia = rsqrt_approx(r2a), ib = rsqrt_approx(r2b);
+          if (GUARD) {
+            ia = r2a > 0.f ? ia : 0.f;
+            ib = r2b > 0.f ? ib : 0.f;
+          }
+          f2 ri = f2make(ia, ib);
+          f2 ri2 = f2mul(ri, ri);
+          f2 mri = f2mul(M, ri);
+          f2 sc = f2mul(mri, ri2);
+          px[p] = f2fma(sc, dx, px[p]);
+          py[p] = f2fma(sc, dy, py[p]);
+          pz[p] = f2fma(sc, dz, pz[p]);
+        }
+      }
+      // Fold this chunk's FP32 partial into the compensated accumulator.
+#pragma unroll
+      for (int p = 0; p < MX_P; p++) {
+        f2 s, e;
+        f2two_sum(hx[p], px[p], s, e);
+        hx[p] = s;
+        lx[p] = f2add(lx[p], e);
+        f2two_sum(hy[p], py[p], s, e);
+        hy[p] = s;
+        ly[p] = f2add(ly[p], e);
+        f2two_sum(hz[p], pz[p], s, e);
+        hz[p] = s;
+        lz[p] = f2add(lz[p], e);
+      }
+    }
+
+    const bool whole = (c0 == 0 && c1 == sk.chunks);
+    if (whole) {
+#pragma unroll
+      for (int p = 0; p < MX_P; p++) {
+        float a[6], b[6];
+        f2split(hx[p], a[0], b[0]);
+        f2split(lx[p], a[1], b[1]);
+        f2split(hy[p], a[2], b[2]);
+        f2split(ly[p], a[3], b[3]);
+        f2split(hz[p], a[4], b[4]);
+        f2split(lz[p], a[5], b[5]);
+        int64_t i0 = t * MX_TILE + (2 * p) * MX_THREADS + tid;
+        int64_t i1 = i0 + MX_THREADS;
+        if (i0 < nt)
+          epi(i0, (double)a[0] + (double)a[1], (double)a[2] + (double)a[3],
+              (double)a[4] + (double)a[5]);
+        if (i1 < nt)
+          epi(i1, (double)b[0] + (double)b[1], (double)b[2] + (double)b[3],
+              (double)b[4] + (double)b[5]);
+      }
+      continue;
+    }
+
+    // Split tile: publish this CTA's partial, count in, last one combines.
+    const int64_t first_tile = u_begin / sk.chunks;
+    float* slot = partials + (2 * g + (t == first_tile ? 0 : 1)) * MX_SLOT_FLOATS;
+#pragma unroll
+    for (int p = 0; p < MX_P; p++) {
+      float a[6], b[6];
+      f2split(hx[p], a[0], b[0]);
+      f2split(lx[p], a[1], b[1]);
+      f2split(hy[p], a[2], b[2]);
+      f2split(ly[p], a[3], b[3]);
+      f2split(hz[p], a[4], b[4]);
+      f2split(lz[p], a[5], b[5]);
+      const int r0 = 2 * p, r1 = 2 * p + 1;
+#pragma unroll
+      for (int q = 0; q < 6; q++) {
+        slot[(int64_t)q * MX_TILE + r0 * MX_THREADS + tid] = a[q];
+        slot[(int64_t)q * MX_TILE + r1 * MX_THREADS + tid] = b[q];
+      }
+    }
+    __threadfence();
+    __syncthreads();
+    const int64_t g_first = sk_owner(sk, t * sk.chunks);
+    const int64_t g_last = sk_owner(sk, t * sk.chunks + sk.chunks - 1);
+    if (tid == 0) {
+      int prev = atomicAdd(&counters[t], 1);
+      s_last = (prev == (int)(g_last - g_first));
+    }
+    __syncthreads();
+    if (!s_last) continue;
+    __threadfence();
+#pragma unroll
+    for (int r = 0; r < MX_R; r++) {
+      const int64_t i = t * MX_TILE + r * MX_THREADS + tid;
+      float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
+      for (int64_t gg = g_first; gg <= g_last; gg++) {
+        const int64_t ft = sk_start(sk, gg) / sk.chunks;
+        const float* sl = partials + (2 * gg + (t == ft ? 0 : 1)) * MX_SLOT_FLOATS;
+#pragma unroll
+        for (int k = 0; k < 3; k++) {
+          float ph = __ldcg(sl + (int64_t)(2 * k) * MX_TILE + r * MX_THREADS + tid);
+          float pl = __ldcg(sl + (int64_t)(2 * k + 1) * MX_TILE + r * MX_THREADS + tid);
+          float s, e;
+          two_sum(h[k], ph, s, e);
+          h[k] = s;
+          l[k] = __fadd_rn(l[k], __fadd_rn(pl, e));
+        }
+      }
+      if (i < nt)
+        epi(i, (double)h[0] + (double)l[0], (double)h[1] + (double)l[1],
+            (double)h[2] + (double)l[2]);
+    }
+    if (tid == 0) counters[t] = 0;  // ready for the next launch
+  }
+}
+
+// Launch helper shared by the force call, the run loop and the no-alloc variant.
+// `grid_cap` bounds the persistent grid (2 slots of partials per CTA in scratch).
+StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap);
+
+}  // namespace gh

@@ -1,0 +1,28 @@
+// Internal C++ interface between the C-ABI layer (capi.cu) and the kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace gh {
+
+// Direct-sum acceleration in code units (G=1, kpc, Msun).  tpos == nullptr means
+// targets are the sources (self term skipped, reference direct_summation).
+int direct_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt,
+                 double eps, int precision, double* acc, cudaStream_t st);
+
+// `nsteps` leapfrog steps with the direct force, one fused launch per step.
+int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
+               double eps, int precision, double* hist_x, double* hist_v, int64_t stride,
+               cudaStream_t st);
+
+// Barnes-Hut acceleration in code units (tpos == nullptr: targets are the sources).
+int tree_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt,
+               double eps, double theta, double* acc, cudaStream_t st);
+
+// `nsteps` leapfrog steps with the tree force (rebuilt every step).
+int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
+             double eps, double theta, double* hist_x, double* hist_v, int64_t stride,
+             cudaStream_t st);
+
+}  // namespace gh

@@ -1,0 +1,78 @@
+"""Device-level API over the C ABI, on torch CUDA tensors.
+
+All tensors are CUDA float64, C-contiguous: positions/velocities (N,3), masses (N).
+Work is enqueued on the given torch stream (the current stream by default).  Forces
+are in code units (G=1, kpc, Msun); leapfrog state is kpc, km/s, Msun, Myr.
+"""
+from __future__ import annotations
+
+import torch
+
+from . import _capi
+
+
+def _check(t, name, shape_tail=None):
+    if not isinstance(t, torch.Tensor):
+        raise TypeError(f"{name} must be a torch tensor")
+    if not t.is_cuda or t.dtype != torch.float64 or not t.is_contiguous():
+        raise ValueError(f"{name} must be a contiguous CUDA float64 tensor")
+    if shape_tail is not None and (t.dim() != 2 or t.shape[1] != shape_tail):
+        raise ValueError(f"{name} must have shape (N,{shape_tail})")
+
+
+def direct_force(pos, mass, eps, force_pos=None, precision="fp64", out=None, stream=None):
+    """Direct-sum acceleration (code units).  ``force_pos=None``: self-force, j != i."""
+    _check(pos, "pos", 3)
+    _check(mass, "mass")
+    if mass.shape[0] != pos.shape[0]:
+        raise ValueError("mass and pos have different lengths")
+    if force_pos is not None:
+        _check(force_pos, "force_pos", 3)
+    n_out = pos.shape[0] if force_pos is None else force_pos.shape[0]
+    if out is None:
+        out = torch.empty((n_out, 3), dtype=torch.float64, device=pos.device)
+    _capi.call("gh_direct_dev", _capi.ptr(pos), _capi.ptr(mass), pos.shape[0], _capi.ptr(force_pos),
+               0 if force_pos is None else force_pos.shape[0], float(eps),
+               _capi.PRECISIONS[precision], _capi.ptr(out), _capi.stream_handle(stream))
+    return out
+
+
+def tree_force(pos, mass, eps, theta=0.7, force_pos=None, out=None, stream=None):
+    """Barnes-Hut acceleration (code units), FP64, reference opening criterion."""
+    _check(pos, "pos", 3)
+    _check(mass, "mass")
+    if mass.shape[0] != pos.shape[0]:
+        raise ValueError("mass and pos have different lengths")
+    if force_pos is not None:
+        _check(force_pos, "force_pos", 3)
+    n_out = pos.shape[0] if force_pos is None else force_pos.shape[0]
+    if out is None:
+        out = torch.empty((n_out, 3), dtype=torch.float64, device=pos.device)
+    _capi.call("gh_tree_dev", _capi.ptr(pos), _capi.ptr(mass), pos.shape[0], _capi.ptr(force_pos),
+               0 if force_pos is None else force_pos.shape[0], float(eps), float(theta),
+               _capi.ptr(out), _capi.stream_handle(stream))
+    return out
+
+
+def run_dkd(pos, vel, mass, nsteps, dt, eps, algorithm="direct", precision="fp64", theta=0.7,
+            hist_stride=0, stream=None):
+    """Advance (pos, vel) in place by ``nsteps`` drift-kick-drift steps on the device.
+
+    Returns ``(hist_pos, hist_vel)`` of shape (nsteps // hist_stride, N, 3) when
+    ``hist_stride > 0``, else None.
+    """
+    _check(pos, "pos", 3)
+    _check(vel, "vel", 3)
+    _check(mass, "mass")
+    n = pos.shape[0]
+    if vel.shape[0] != n or mass.shape[0] != n:
+        raise ValueError("pos, vel and mass have different lengths")
+    hp = hv = None
+    if hist_stride > 0:
+        ns = nsteps // hist_stride
+        hp = torch.empty((ns, n, 3), dtype=torch.float64, device=pos.device)
+        hv = torch.empty((ns, n, 3), dtype=torch.float64, device=pos.device)
+    _capi.call("gh_run_dkd", _capi.ptr(pos), _capi.ptr(vel), _capi.ptr(mass), n, int(nsteps), float(dt),
+               float(eps), _capi.ALGORITHMS[algorithm], _capi.PRECISIONS[precision], float(theta),
+               _capi.ptr(hp), _capi.ptr(hv), int(hist_stride), _capi.stream_handle(stream))
+    return (hp, hv) if hist_stride > 0 else None

@@ -1,0 +1,434 @@
+"""Host API mirroring ``gravhopper.gravhopper``: ``Simulation``, ``IC`` and the exceptions.
+
+The names, arguments, defaults and state layout follow gravhopper/gravhopper.py:68-1785:
+``Simulation(dt, eps, algorithm='tree')``, ``add_IC``, ``run(N)``, ``reset``, ``snap``,
+``current_snap``, ``prev_snap``, ``perform_timestep``, ``calculate_acceleration``,
+``add_external_force`` (and the time- and velocity-dependent variants),
+``positions``/``velocities`` of shape (Nsnap, Np, 3), ``masses`` (Np), ``times`` (Nsnap).
+
+What differs is where the work runs: ``run`` keeps the particles on the GPU and
+executes every drift-kick-drift step (gravhopper.py:405-416) there, one fused launch
+per step, writing each step's state into device history buffers that are copied to
+the host once per call.  When external forces are registered, each step falls back to
+the host for those callbacks (they are arbitrary Python), with the N-body force still
+computed on the GPU.
+
+Extensions: ``theta`` (opening angle, default 0.7 as gravhopper/jbgrav.py:52) and
+``precision`` ('fp64' default; 'mixed' for the direct sum).
+
+Units: with astropy importable, Quantities in and out as in the reference; otherwise
+plain numbers in kpc, km/s, Msun, Myr.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from . import ics as _ics
+from . import jbgrav
+from . import units as U
+
+
+class GravHopperException(Exception):
+    """Parent class for all error exceptions."""
+
+
+class UninitializedSimulationException(GravHopperException):
+    """Exception for trying to run a simulation without any initial conditions."""
+
+
+class ICException(GravHopperException):
+    """Exception for trying to add ICs that don't make sense."""
+
+    def __init__(self, msg):
+        super().__init__(msg)
+        print(msg)
+
+
+class UnknownAlgorithmException(GravHopperException):
+    """Exception for using an unknown N-body algorithm name."""
+
+
+class ExternalPackageException(GravHopperException):
+    """Exception for calling a pynbody/galpy/gala/agama function when not using them."""
+
+    def __init__(self, msg):
+        super().__init__(msg)
+        print(msg)
+
+
+def _default(q_astropy, plain):
+    return q_astropy() if U.HAVE_ASTROPY else plain
+
+
+class Simulation(object):
+    """Main class for an N-body simulation (gravhopper/gravhopper.py:91-163)."""
+
+    def __init__(self, dt=None, eps=None, algorithm="tree", theta=0.7, precision="fp64"):
+        if dt is None:
+            dt = _default(lambda: 1 * U._u.Myr, 1.0)
+        if eps is None:
+            eps = _default(lambda: 100 * U._u.pc, 0.1)
+        self.ICarrays = False
+        self.Np = 0
+        self.Nsnap = 0
+        self.timestep = 0
+        self.running = False
+        self._pos = None   # (Nsnap, Np, 3) kpc
+        self._vel = None   # (Nsnap, Np, 3) km/s
+        self._mass = None  # (Np) Msun
+        self._times = None  # (Nsnap) Myr
+        self.extra_force_functions = []
+        self.extra_timedependent_force_functions = []
+        self.extra_velocitydependent_force_functions = []
+        self.lenunit, self.velunit, self.massunit, self.timeunit = U.LENGTH, U.VELOCITY, U.MASS, U.TIME
+        self.accelunit = U.ACCEL
+        self.params = {}
+        self.set_dt(dt)
+        self.set_eps(eps)
+        self.set_algorithm(algorithm)
+        self.set_theta(theta)
+        self.set_precision(precision)
+
+    # ---- parameters (gravhopper.py:166-290) ----------------------------------
+    def set_dt(self, dt):
+        """Sets the simulation time step (time dimensions; plain numbers are Myr)."""
+        U.value(dt, U.TIME, "dt")
+        self.params["dt"] = dt
+
+    def get_dt(self):
+        return self.params["dt"]
+
+    def set_eps(self, eps):
+        """Sets the gravitational softening length (plain numbers are kpc)."""
+        U.value(eps, U.LENGTH, "eps")
+        self.params["eps"] = eps
+
+    def get_eps(self):
+        return self.params["eps"]
+
+    def set_algorithm(self, algorithm):
+        """'tree' (Barnes-Hut) or 'direct' (direct summation)."""
+        if algorithm in ("tree", "direct"):
+            self.params["algorithm"] = algorithm
+        else:
+            raise ValueError("algorithm must be 'tree' or 'direct'.")
+
+    def get_algorithm(self):
+        return self.params["algorithm"]
+
+    def set_theta(self, theta):
+        """Opening angle of the tree walk in radians (default 0.7)."""
+        theta = float(theta)
+        if not theta >= 0.0:
+            raise ValueError("theta must be >= 0.")
+        self.params["theta"] = theta
+
+    def get_theta(self):
+        return self.params["theta"]
+
+    def set_precision(self, precision):
+        """'fp64' (reference arithmetic) or 'mixed' (FP32 pairs, direct sum only)."""
+        if precision not in ("fp64", "mixed"):
+            raise ValueError("precision must be 'fp64' or 'mixed'.")
+        self.params["precision"] = precision
+
+    def get_precision(self):
+        return self.params["precision"]
+
+    def _dt(self):
+        return float(U.value(self.params["dt"], U.TIME, "dt"))
+
+    def _eps(self):
+        return float(U.value(self.params["eps"], U.LENGTH, "eps"))
+
+    # ---- state arrays ------------------------------------------------------------
+    @property
+    def positions(self):
+        return None if self._pos is None else U.quantity(self._pos, U.LENGTH)
+
+    @property
+    def velocities(self):
+        return None if self._vel is None else U.quantity(self._vel, U.VELOCITY)
+
+    @property
+    def masses(self):
+        return None if self._mass is None else U.quantity(self._mass, U.MASS)
+
+    @property
+    def times(self):
+        return None if self._times is None else U.quantity(self._times, U.TIME)
+
+    # ---- running (gravhopper.py:293-342) ---------------------------------------
+    def run(self, N=1):
+        """Run N timesteps; initialises on the first call, continues afterwards."""
+        N = int(N)
+        if not self.running:
+            self.init_run(N)
+        else:
+            self.Nsnap += N
+            self._pos = np.concatenate((self._pos, np.zeros((N, self.Np, 3))), axis=0)
+            self._vel = np.concatenate((self._vel, np.zeros((N, self.Np, 3))), axis=0)
+            self._times = np.concatenate((self._times, np.zeros(N)), axis=0)
+        if self._has_extra_forces():
+            for _ in range(N):
+                self.timestep += 1
+                self.perform_timestep()
+                self._times[self.timestep] = self._times[self.timestep - 1] + self._dt()
+            return
+        self._run_device(N)
+
+    def _has_extra_forces(self):
+        return bool(self.extra_force_functions or self.extra_timedependent_force_functions
+                    or self.extra_velocitydependent_force_functions)
+
+    def _run_device(self, N):
+        import torch
+
+        from . import engine
+        if N <= 0:
+            return
+        t0 = self.timestep
+        dev = torch.device("cuda", torch.cuda.current_device())
+        x = torch.from_numpy(np.ascontiguousarray(self._pos[t0])).to(dev)
+        v = torch.from_numpy(np.ascontiguousarray(self._vel[t0])).to(dev)
+        m = torch.from_numpy(np.ascontiguousarray(self._mass)).to(dev)
+        hist = engine.run_dkd(x, v, m, N, self._dt(), self._eps(), algorithm=self.params["algorithm"],
+                              precision=self.params["precision"], theta=self.params["theta"],
+                              hist_stride=1)
+        hp, hv = hist
+        self._pos[t0 + 1:t0 + N + 1] = hp.cpu().numpy()
+        self._vel[t0 + 1:t0 + N + 1] = hv.cpu().numpy()
+        dt = self._dt()
+        for k in range(t0 + 1, t0 + N + 1):
+            self._times[k] = self._times[k - 1] + dt
+        self.timestep = t0 + N
+
+    def init_run(self, Nsnap=None):
+        """Initialise an N-body run (gravhopper.py:324-342)."""
+        if self.ICarrays is False:
+            raise UninitializedSimulationException
+        self.Nsnap = Nsnap + 1
+        self.Np = len(self.ICarrays["pos"])
+        self._pos = np.zeros((self.Nsnap, self.Np, 3))
+        self._vel = np.zeros((self.Nsnap, self.Np, 3))
+        self._mass = np.zeros(self.Np)
+        self._times = np.zeros(self.Nsnap)
+        self._pos[0] = U.value(self.ICarrays["pos"], U.LENGTH, "pos")
+        self._vel[0] = U.value(self.ICarrays["vel"], U.VELOCITY, "vel")
+        self._mass[:] = U.value(self.ICarrays["mass"], U.MASS, "mass")
+        self.running = True
+
+    def reset(self):
+        """Back to the state before init_run(); ICs and external forces are kept."""
+        self.running = False
+        self._pos = self._vel = self._mass = self._times = None
+        self.Nsnap = 0
+        self.timestep = 0
+
+    def snap(self, step):
+        """dict with 'pos' (Np,3), 'vel' (Np,3), 'mass' (Np) of snapshot ``step``."""
+        return {"pos": U.quantity(self._pos[step], U.LENGTH), "vel": U.quantity(self._vel[step], U.VELOCITY),
+                "mass": U.quantity(self._mass, U.MASS)}
+
+    def current_snap(self):
+        return self.snap(self.timestep)
+
+    def prev_snap(self):
+        return self.snap(self.timestep - 1)
+
+    def perform_timestep(self):
+        """One DKD step from snapshot timestep-1 into snapshot timestep (gravhopper.py:405-416)."""
+        t = self.timestep
+        dt = self._dt()
+        x0, v0 = self._pos[t - 1], self._vel[t - 1]
+        self._pos[t] = x0 + ((0.5 * v0) * dt) * U.KMS_MYR_TO_KPC
+        kick_time = self._times[t - 1] + 0.5 * dt
+        acc = np.asarray(U.value(self.calculate_acceleration(time=U.quantity(kick_time, U.TIME)),
+                                 U.ACCEL, "acceleration"))
+        self._vel[t] = v0 + acc * dt
+        self._pos[t] = self._pos[t] + ((0.5 * self._vel[t]) * dt) * U.KMS_MYR_TO_KPC
+
+    def calculate_acceleration(self, time=None):
+        """N-body plus external acceleration at current_snap() (gravhopper.py:419-459)."""
+        snap = self.current_snap()
+        if self.Np > 1:
+            if self.params["algorithm"] == "direct":
+                nbody = jbgrav.direct_summation(snap, self.params["eps"], precision=self.params["precision"])
+            elif self.params["algorithm"] == "tree":
+                nbody = jbgrav.tree_force(snap, self.params["eps"], theta=self.params["theta"])
+            else:
+                raise UnknownAlgorithmException()
+        else:
+            nbody = U.quantity(np.zeros((self.Np, 3)), U.ACCEL)
+        extra = self.calculate_extra_acceleration(snap["pos"], nbody, time=time,
+                                                  vel=self.prev_snap()["vel"])
+        return nbody + extra
+
+    def calculate_extra_acceleration(self, pos, template_array, time=None, vel=None):
+        """Sum of the registered external forces (gravhopper.py:462-473)."""
+        ext = np.zeros_like(template_array)
+        for fn, args in self.extra_force_functions:
+            ext += fn(pos, args)
+        for fn, args in self.extra_timedependent_force_functions:
+            ext += fn(pos, time, args)
+        for fn, args in self.extra_velocitydependent_force_functions:
+            ext += fn(pos, vel, args)
+        return ext
+
+    # ---- external forces (gravhopper.py:603-845): plain callables -----------------
+    def add_external_force(self, fn, args=None, agama_units=None):
+        """Add a position-dependent force ``fn(pos, args)`` (km/s/Myr when unitless)."""
+        if isinstance(fn, list):
+            for item in fn:
+                self.add_external_force(item, args)
+            return
+        if not callable(fn):
+            raise ExternalPackageException("Only callables are supported as external forces here.")
+        self.extra_force_functions.append((fn, args))
+
+    def add_external_timedependent_force(self, fn, agama_units=None, args=None):
+        """Add a time-dependent force ``fn(pos, time, args)``."""
+        if isinstance(fn, list):
+            for item in fn:
+                self.add_external_timedependent_force(item, args=args)
+            return
+        if not callable(fn):
+            raise ExternalPackageException("Only callables are supported as external forces here.")
+        self.extra_timedependent_force_functions.append((fn, args))
+
+    def add_external_velocitydependent_force(self, fn, args=None):
+        """Add a velocity-dependent force ``fn(pos, vel, args)``."""
+        if isinstance(fn, list):
+            for item in fn:
+                self.add_external_velocitydependent_force(item, args)
+            return
+        if not callable(fn):
+            raise ExternalPackageException("Only callables are supported as external forces here.")
+        self.extra_velocitydependent_force_functions.append((fn, args))
+
+    # ---- initial conditions (gravhopper.py:848-904) --------------------------------
+    def nrows(self, array):
+        return array.shape[0] if np.ndim(array) > 1 else 1
+
+    def add_IC(self, newIC):
+        """Append particles: dict with 'pos', 'vel' (Np,3) and 'mass' (Np)."""
+        if "pos" not in newIC:
+            raise ICException("Missing 'pos' key in initial conditions function.")
+        if "vel" not in newIC:
+            raise ICException("Missing 'vel' key in initial conditions function.")
+        if "mass" not in newIC:
+            raise ICException("Missing 'mass' key in initial conditions function.")
+        npos = self.nrows(newIC["pos"])
+        nvel = self.nrows(newIC["vel"])
+        nmass = len(newIC["mass"])
+        if (npos != nvel) | (npos != nmass):
+            raise ICException("Inconsistent number of particles in initial conditions function.")
+        if self.ICarrays is False:
+            self.ICarrays = {"pos": newIC["pos"], "vel": newIC["vel"], "mass": newIC["mass"]}
+        else:
+            self.ICarrays["pos"] = np.vstack((self.ICarrays["pos"], newIC["pos"]))
+            self.ICarrays["vel"] = np.vstack((self.ICarrays["vel"], newIC["vel"]))
+            self.ICarrays["mass"] = np.hstack((self.ICarrays["mass"], newIC["mass"]))
+
+
+class IC(object):
+    """Initial-condition generators (subset of gravhopper/gravhopper.py:1167-1734).
+
+    Plain numbers are kpc, km/s, Msun.  Each returns {'pos', 'vel', 'mass'}.
+    """
+
+    @staticmethod
+    def _finish(pos, vel, mass, center_pos, center_vel, force_origin):
+        pos, vel = force_centers(pos, vel, center_pos, center_vel, force_origin)
+        return {"pos": U.quantity(pos, U.LENGTH), "vel": U.quantity(vel, U.VELOCITY),
+                "mass": U.quantity(mass, U.MASS)}
+
+    @staticmethod
+    def Plummer(N=None, b=None, totmass=None, center_pos=None, center_vel=None, force_origin=True,
+                seed=None):
+        """Isotropic Plummer sphere (gravhopper.py:1404-1493): speeds from q drawn by an
+        inverse-CDF table of q^2 (1-q^2)^(7/2) on a 0.01 grid, as the reference does."""
+        if N is None or b is None or totmass is None:
+            raise ICException("Plummer requires N, b, and totmass.")
+        b = float(U.value(b, U.LENGTH, "b"))
+        M = float(U.value(totmass, U.MASS, "totmass"))
+        rng = np.random.default_rng(seed)
+        xi = rng.uniform(0.0, 1.0, size=N)
+        r = b / np.sqrt(xi ** (-2.0 / 3) - 1)
+        cth = rng.uniform(-1.0, 1.0, size=N)
+        ph = rng.uniform(0.0, 2.0 * np.pi, size=N)
+        sth = np.sqrt(1.0 - cth ** 2)
+        pos = np.stack([r * sth * np.cos(ph), r * sth * np.sin(ph), r * cth], axis=1)
+        qax = np.arange(0, 1.01, 0.01)
+        cdf = np.cumsum(qax ** 2 * (1.0 - qax ** 2) ** 3.5)
+        cdf /= cdf[-1]
+        q = np.interp(rng.uniform(0.0, 1.0, size=N), cdf, qax)
+        speed = q * np.sqrt(2.0 * U.G_KPC_KMS2_MSUN * M / b) * (1.0 + (r / b) ** 2) ** (-0.25)
+        cvt = rng.uniform(-1.0, 1.0, size=N)
+        vph = rng.uniform(0.0, 2.0 * np.pi, size=N)
+        svt = np.sqrt(1.0 - cvt ** 2)
+        vel = np.stack([speed * svt * np.cos(vph), speed * svt * np.sin(vph), speed * cvt], axis=1)
+        return IC._finish(pos, vel, np.full(N, M / N), center_pos, center_vel, force_origin)
+
+    @staticmethod
+    def TSIS(N=None, maxrad=None, totmass=None, center_pos=None, center_vel=None, force_origin=True,
+             seed=None):
+        """Truncated singular isothermal sphere (gravhopper.py:1327-1400)."""
+        if N is None or maxrad is None or totmass is None:
+            raise ICException("TSIS requires N, maxrad, and totmass.")
+        R = float(U.value(maxrad, U.LENGTH, "maxrad"))
+        M = float(U.value(totmass, U.MASS, "totmass"))
+        rng = np.random.default_rng(seed)
+        sigma = np.sqrt(M * U.G_KPC_KMS2_MSUN / (2 * R))
+        r = rng.uniform(0.0, R, size=N)
+        cth = rng.uniform(-1.0, 1.0, size=N)
+        ph = rng.uniform(0.0, 2.0 * np.pi, size=N)
+        sth = np.sqrt(1.0 - cth ** 2)
+        pos = np.stack([r * sth * np.cos(ph), r * sth * np.sin(ph), r * cth], axis=1)
+        vel = np.stack([rng.normal(0.0, sigma, size=N) for _ in range(3)], axis=1)
+        return IC._finish(pos, vel, np.full(N, M / N), center_pos, center_vel, force_origin)
+
+    @staticmethod
+    def Hernquist(N=None, a=None, totmass=None, cutoff=10.0, center_pos=None, center_vel=None,
+                  force_origin=True, seed=None):
+        """Hernquist sphere truncated at ``cutoff`` scale radii.  Velocities are Gaussian
+        with the isotropic Jeans dispersion (the reference samples the distribution
+        function instead, gravhopper.py:1497-1607)."""
+        if N is None or a is None or totmass is None:
+            raise ICException("Hernquist requires N, a, and totmass.")
+        a = float(U.value(a, U.LENGTH, "a"))
+        M = float(U.value(totmass, U.MASS, "totmass"))
+        rng = np.random.default_rng(seed)
+        xi = rng.uniform(0.0, cutoff ** 2 / (1.0 + cutoff) ** 2, size=N)
+        r = a / (1.0 / np.sqrt(xi) - 1.0)
+        cth = rng.uniform(-1.0, 1.0, size=N)
+        ph = rng.uniform(0.0, 2.0 * np.pi, size=N)
+        sth = np.sqrt(1.0 - cth ** 2)
+        pos = np.stack([r * sth * np.cos(ph), r * sth * np.sin(ph), r * cth], axis=1)
+        sig = np.sqrt(_ics.hernquist_sigma2(r, a, M))
+        vel = sig[:, None] * rng.normal(size=(N, 3))
+        return IC._finish(pos, vel, np.full(N, M / N), center_pos, center_vel, force_origin)
+
+    @staticmethod
+    def from_galpy_df(*args, **kwargs):
+        raise ExternalPackageException("galpy is not available to use from_galpy_df()")
+
+    @staticmethod
+    def from_pyn_snap(*args, **kwargs):
+        raise ExternalPackageException("Could not import pynbody to use from_pyn_snap()")
+
+
+def force_centers(positions, velocities, center_pos=None, center_vel=None, force_origin=True):
+    """Shift to the requested centre of mass and mean velocity (gravhopper.py:1740-1785)."""
+    newpos = np.array(U.value(positions, U.LENGTH, "positions"), dtype=np.float64)
+    newvel = np.array(U.value(velocities, U.VELOCITY, "velocities"), dtype=np.float64)
+    if force_origin:
+        if center_pos is None:
+            center_pos = np.zeros(3)
+        if center_vel is None:
+            center_vel = np.zeros(3)
+    if center_pos is not None:
+        newpos += np.asarray(U.value(center_pos, U.LENGTH, "center_pos")) - newpos.mean(axis=0)
+    if center_vel is not None:
+        newvel += np.asarray(U.value(center_vel, U.VELOCITY, "center_vel")) - newvel.mean(axis=0)
+    return newpos, newvel

@@ -1,0 +1,108 @@
+/*
+ * gravhopper_gb300.h -- C ABI of the GB300 gravity engine (libgravhopper_gb300.so).
+ *
+ * Plain pointers and sizes only.  Units: code units G=1, length kpc, mass Msun for
+ * forces (as gravhopper/_jbgrav.c:137-139); the leapfrog entry points take positions
+ * in kpc, velocities in km/s and times in Myr (gravhopper/gravhopper.py:146-151).
+ * Arrays of vectors are (N,3) C-contiguous float64, masses (N) float64.
+ *
+ * Every function returns GH_OK (0) or an error code; gh_last_error() gives the
+ * message of the calling thread's last failure.
+ *
+ * "host" entry points take host pointers, copy to the device, compute and copy back
+ * before returning.  "_dev" entry points take device pointers and a cudaStream_t
+ * (passed as void*, NULL = legacy default stream) and are stream-ordered: they return
+ * once the work is enqueued.  The library keeps one grow-only device workspace per
+ * device; calls that use it must not run concurrently on different streams.
+ */
+#ifndef GRAVHOPPER_GB300_H
+#define GRAVHOPPER_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GH_VERSION 100
+
+/* status codes */
+#define GH_OK 0
+#define GH_ERR_ARG 1       /* invalid argument: negative size, NULL buffer, unknown enum */
+#define GH_ERR_SHAPE 2     /* inconsistent shapes (host mirrors raise RuntimeError) */
+#define GH_ERR_OOM 3       /* device allocation failed */
+#define GH_ERR_DEPTH 4     /* octree deeper than supported: coincident particles */
+#define GH_ERR_TIMEOUT 5   /* a bounded device-side wait gave up */
+#define GH_ERR_CUDA 6      /* CUDA runtime error */
+#define GH_ERR_NO_DEVICE 7 /* no usable CUDA device */
+
+/* precision of the direct-sum pair arithmetic */
+#define GH_PREC_FP64 0  /* FP64 throughout, bit-exact with the reference's operation order */
+#define GH_PREC_MIXED 1 /* FP32 pairs, compensated per-particle accumulation, FP64 state */
+
+/* force algorithm, as Simulation.params['algorithm'] (gravhopper/gravhopper.py:255-274) */
+#define GH_ALGO_DIRECT 0
+#define GH_ALGO_TREE 1
+
+/* ---- library ------------------------------------------------------------------ */
+const char* gh_last_error(void);
+int gh_version(void);
+/* Number of kernels this library has launched since load (all threads). */
+int64_t gh_launch_count(void);
+
+/* ---- host-buffer drop-ins for the reference module gravhopper._jbgrav --------- */
+
+/* Replaces _jbgrav.direct_summation(pos, mass, eps), gravhopper/_jbgrav.c:68-193.
+ * pos (np,3), mass (np) -> out (np,3) in code units.  FP64, bit-exact. */
+int gh_direct_summation(const double* pos, const double* mass, int64_t np, double eps,
+                        double* out);
+
+/* Replaces _jbgrav.direct_summation_position(pos, mass, force_pos, eps),
+ * gravhopper/_jbgrav.c:200-353.  force_pos (nf,3) -> out (nf,3).  A target that
+ * coincides with a particle when eps == 0 gets no term from it (r^2+eps^2 == 0). */
+int gh_direct_summation_position(const double* pos, const double* mass, int64_t np,
+                                 const double* force_pos, int64_t nf, double eps, double* out);
+
+/* Direct sum with a precision choice (GH_PREC_*).  force_pos == NULL: targets are
+ * the particles themselves and the self term is skipped (direct_summation). */
+int gh_direct_host(const double* pos, const double* mass, int64_t np, const double* force_pos,
+                   int64_t nf, double eps, int precision, double* out);
+
+/* ---- device-pointer, stream-ordered ------------------------------------------- */
+
+/* Direct-sum acceleration (code units) into acc (nf,3), or (np,3) when
+ * force_pos == NULL (self term skipped). */
+int gh_direct_dev(const double* pos, const double* mass, int64_t np, const double* force_pos,
+                  int64_t nf, double eps, int precision, double* acc, void* stream);
+
+/* Advances (pos, vel) in place by nsteps drift-kick-drift leapfrog steps
+ * (Simulation.perform_timestep, gravhopper/gravhopper.py:405-416): pos [kpc],
+ * vel [km/s], mass [Msun], dt [Myr], eps [kpc].  algorithm GH_ALGO_DIRECT uses
+ * `precision`; GH_ALGO_TREE uses `theta` (FP64 walk).  When hist_pos/hist_vel are
+ * non-NULL, the state after every hist_stride-th step is written to consecutive
+ * (np,3) slots of them (nsteps/hist_stride slots). */
+int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t nsteps,
+               double dt, double eps, int algorithm, int precision, double theta,
+               double* hist_pos, double* hist_vel, int64_t hist_stride, void* stream);
+
+/* ---- diagnostics -------------------------------------------------------------- */
+
+/* Measures the current device's FMA-pipe throughput with dependent-chain kernels
+ * (no counterpart in the reference): FP32 (packed f32x2) and FP64 FMA lane-operations
+ * per second; either pointer may be NULL.  Used as roofline denominators. */
+int gh_measure_fma_peaks(double* fp32_lane_ops_per_s, double* fp64_lane_ops_per_s, void* stream);
+
+/* Enables (1) or disables (0) CUDA-event timing of every force-kernel launch (direct
+ * FP64, direct mixed, tree walk) on the stream it is launched on (no counterpart in
+ * the reference). */
+int gh_kernel_timing(int enable);
+
+/* Synchronises on and sums the recorded launch durations since the last collect:
+ * total milliseconds and number of timed launches; clears the record. */
+int gh_kernel_timing_collect(double* total_ms, int64_t* launches);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GRAVHOPPER_GB300_H */

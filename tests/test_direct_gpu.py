@@ -1,0 +1,108 @@
+"""Direct-sum parity on the GPU, through the C ABI.
+
+FP64 form: bit-exact against the reference's own outputs (golden vectors) and the
+oracle.  Mixed form: rms relative acceleration error <= 1e-6 against the FP64 oracle
+(the engine's stated tolerance), max relative error <= 1e-3 (particles whose net
+acceleration nearly cancels), and bit-for-bit reproducible between calls.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+MIXED_RMS_TOL = 1e-6
+MIXED_MAX_TOL = 1e-3
+
+
+def rel_err(a, ref):
+    num = np.linalg.norm(a - ref, axis=1)
+    den = np.linalg.norm(ref, axis=1)
+    r = num / np.where(den > 0, den, 1.0)
+    return float(np.sqrt(np.mean(r * r))), float(r.max())
+
+
+def test_fp64_direct_bitexact_golden(golden, lib, cuda):
+    from gravhopper_gb300 import _jbgrav
+    keys = sorted(k[:-4] for k in golden if k.startswith("direct_") and k.endswith("_out"))
+    for k in keys:
+        got = _jbgrav.direct_summation(golden[k + "_pos"], golden[k + "_mass"], float(golden[k + "_eps"]))
+        np.testing.assert_array_equal(got, golden[k + "_out"], err_msg=k)
+    got = _jbgrav.direct_summation(golden["plummer_pos"], golden["plummer_mass"], 5e-5)
+    np.testing.assert_array_equal(got, golden["plummer_force"])
+
+
+def test_fp64_direct_position_bitexact_golden(golden, lib, cuda):
+    from gravhopper_gb300 import _jbgrav
+    for tag in ("eps", "eps0"):
+        k = f"dpos_{tag}"
+        got = _jbgrav.direct_summation_position(golden[k + "_pos"], golden[k + "_mass"], golden[k + "_fpos"],
+                                                float(golden[k + "_eps"]))
+        np.testing.assert_array_equal(got, golden[k + "_out"])
+
+
+@pytest.mark.parametrize("n", [257, 1000, 4099])
+def test_fp64_direct_bitexact_oracle(lib, cuda, n):
+    from gravhopper_gb300 import _jbgrav
+    rng = np.random.default_rng(n)
+    pos = rng.standard_cauchy(size=(n, 3)) * 1e-2
+    mass = rng.uniform(0.1, 10.0, size=n)
+    np.testing.assert_array_equal(_jbgrav.direct_summation(pos, mass, 1e-3),
+                                  oracle.direct_summation(pos, mass, 1e-3))
+    fp = np.concatenate([pos[:5], rng.normal(size=(77, 3))])
+    np.testing.assert_array_equal(_jbgrav.direct_summation_position(pos, mass, fp, 0.0),
+                                  oracle.direct_summation_position(pos, mass, fp, 0.0))
+
+
+def test_fp64_device_api_matches_host_api(lib, cuda):
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    ic = ics.plummer(3000, seed=9)
+    x = torch.from_numpy(ic["pos"]).to(cuda)
+    m = torch.from_numpy(ic["mass"]).to(cuda)
+    a = engine.direct_force(x, m, 5e-5).cpu().numpy()
+    np.testing.assert_array_equal(a, oracle.direct_summation(ic["pos"], ic["mass"], 5e-5))
+
+
+@pytest.mark.parametrize("n", [2000, 5000, 16384, 65536])
+def test_mixed_direct_accuracy(lib, cuda, n):
+    from gravhopper_gb300 import _jbgrav, ics
+    ic = ics.plummer(n, seed=n)
+    ref = oracle.direct_summation(ic["pos"], ic["mass"], 5e-5)
+    got = _jbgrav.direct_summation_mixed(ic["pos"], ic["mass"], 5e-5)
+    rms, mx = rel_err(got, ref)
+    assert rms <= MIXED_RMS_TOL, (rms, mx)
+    assert mx <= MIXED_MAX_TOL, (rms, mx)
+    again = _jbgrav.direct_summation_mixed(ic["pos"], ic["mass"], 5e-5)
+    np.testing.assert_array_equal(got, again)  # deterministic split-tile combine
+
+
+def test_mixed_position_and_zero_softening(lib, cuda):
+    from gravhopper_gb300 import _jbgrav, ics
+    ic = ics.plummer(3000, seed=4)
+    rng = np.random.default_rng(1)
+    fp = np.concatenate([ic["pos"][:10], rng.normal(size=(500, 3)) * 2e-3])
+    ref = oracle.direct_summation_position(ic["pos"], ic["mass"], fp, 0.0)
+    got = _jbgrav.direct_summation_mixed(ic["pos"], ic["mass"], 0.0, force_pos=fp)
+    assert np.isfinite(got).all()
+    rms, mx = rel_err(got, ref)
+    assert rms <= 1e-5, (rms, mx)
+
+
+def test_empty_and_tiny_inputs(lib, cuda):
+    from gravhopper_gb300 import _jbgrav
+    assert _jbgrav.direct_summation(np.zeros((0, 3)), np.zeros(0), 0.1).shape == (0, 3)
+    one = _jbgrav.direct_summation(np.ones((1, 3)), np.ones(1), 0.1)
+    np.testing.assert_array_equal(one, np.zeros((1, 3)))
+    got = _jbgrav.direct_summation_position(np.zeros((0, 3)), np.zeros(0), np.ones((4, 3)), 0.1)
+    np.testing.assert_array_equal(got, np.zeros((4, 3)))
+    got = _jbgrav.direct_summation_mixed(np.ones((1, 3)), np.ones(1), 0.1)
+    np.testing.assert_array_equal(got, np.zeros((1, 3)))
+
+
+def test_invalid_arguments_raise(lib, cuda):
+    from gravhopper_gb300 import _capi, _jbgrav
+    with pytest.raises(_capi.EngineError):
+        _jbgrav.direct_summation(np.zeros((3, 3)), np.ones(3), -1.0)

@@ -1,0 +1,73 @@
+"""Leapfrog runs on the GPU against the reference trajectory.
+
+FP64 direct: every step is bit-identical to the NumPy restatement of
+Simulation.perform_timestep driven by the reference's compiled direct sum (golden
+snapshots after 100, 200, 300, 400 steps).  Mixed: relative energy drift over the
+400-step run <= 1e-5 and positions within 1e-6 kpc of the FP64 run.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def _state(golden, cuda):
+    import torch
+    x = torch.from_numpy(golden["plummer_pos"].copy()).to(cuda)
+    v = torch.from_numpy(golden["plummer_vel"].copy()).to(cuda)
+    m = torch.from_numpy(golden["plummer_mass"].copy()).to(cuda)
+    return x, v, m
+
+
+def test_fp64_run_bitexact_400_steps(golden, lib, cuda):
+    from gravhopper_gb300 import engine
+    x, v, m = _state(golden, cuda)
+    hp, hv = engine.run_dkd(x, v, m, 400, 0.005, 5e-5, algorithm="direct", precision="fp64",
+                            hist_stride=100)
+    for k in range(4):
+        np.testing.assert_array_equal(hp[k].cpu().numpy(), golden[f"traj_direct_x_{(k + 1) * 100}"])
+        np.testing.assert_array_equal(hv[k].cpu().numpy(), golden[f"traj_direct_v_{(k + 1) * 100}"])
+    np.testing.assert_array_equal(x.cpu().numpy(), golden["traj_direct_x_400"])
+
+
+def test_simulation_api_matches_reference(golden, lib, cuda):
+    import gravhopper_gb300 as gh
+    sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct")
+    sim.add_IC({"pos": golden["plummer_pos"], "vel": golden["plummer_vel"], "mass": golden["plummer_mass"]})
+    sim.run(60)
+    sim.run(40)  # continue-run semantics (gravhopper.py:303-314)
+    assert sim.positions.shape == (101, 2000, 3)
+    np.testing.assert_array_equal(sim.positions[100], golden["traj_direct_x_100"])
+    np.testing.assert_array_equal(sim.velocities[100], golden["traj_direct_v_100"])
+    np.testing.assert_allclose(sim.times[100], 0.5, rtol=1e-12)
+
+
+def test_mixed_run_energy_drift(golden, lib, cuda):
+    from gravhopper_gb300 import engine
+    x, v, m = _state(golden, cuda)
+    e0 = oracle.total_energy(golden["plummer_pos"], golden["plummer_vel"], golden["plummer_mass"], 5e-5)
+    engine.run_dkd(x, v, m, 400, 0.005, 5e-5, algorithm="direct", precision="mixed")
+    xf, vf = x.cpu().numpy(), v.cpu().numpy()
+    e1 = oracle.total_energy(xf, vf, golden["plummer_mass"], 5e-5)
+    e_ref = oracle.total_energy(golden["traj_direct_x_400"], golden["traj_direct_v_400"],
+                                golden["plummer_mass"], 5e-5)
+    assert abs(e1 - e0) / abs(e0) <= 1e-5
+    # the mixed run tracks the FP64 reference trajectory's energy to well below its own drift
+    assert abs(e1 - e_ref) / abs(e0) <= 1e-6
+    assert np.abs(xf - golden["traj_direct_x_400"]).max() < 1e-6
+
+
+def test_single_particle_and_empty_runs(lib, cuda):
+    import torch
+
+    from gravhopper_gb300 import engine
+    x = torch.tensor([[1.0, 2.0, 3.0]], dtype=torch.float64, device=cuda)
+    v = torch.tensor([[10.0, 0.0, 0.0]], dtype=torch.float64, device=cuda)
+    m = torch.tensor([5.0], dtype=torch.float64, device=cuda)
+    engine.run_dkd(x, v, m, 3, 0.1, 0.0, algorithm="direct", precision="fp64")
+    ref_x, ref_v = oracle.dkd_run(np.array([[1.0, 2.0, 3.0]]), np.array([[10.0, 0.0, 0.0]]), np.array([5.0]),
+                                  0.1, 0.0, 3)
+    np.testing.assert_array_equal(x.cpu().numpy(), ref_x)
+    np.testing.assert_array_equal(v.cpu().numpy(), ref_v)
