@@ -65,6 +65,9 @@ SIGNATURES = {
     "gh_direct_summation": (_int, [_vp, _vp, _i64, _dbl, _vp]),
     "gh_direct_summation_position": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _vp]),
     "gh_direct_host": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _int, _vp]),
+    "gh_tree_force": (_int, [_vp, _vp, _i64, _dbl, _dbl, _vp]),
+    "gh_tree_force_position": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _vp]),
+    "gh_tree_dev": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _vp, _vp]),
     "gh_direct_dev": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _int, _vp, _vp]),
     "gh_run_dkd": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _int, _dbl, _vp, _vp, _i64,
                           _vp]),

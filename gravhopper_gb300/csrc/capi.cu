@@ -93,6 +93,24 @@ int gh_direct_summation_position(const double* pos, const double* mass, int64_t 
   return host_call(HK_DIRECT, pos, mass, np, force_pos, nf, eps, GH_PREC_FP64, 0.0, out);
 }
 
+int gh_tree_force(const double* pos, const double* mass, int64_t np, double eps, double theta,
+                  double* out) {
+  return host_call(HK_TREE, pos, mass, np, nullptr, 0, eps, GH_PREC_FP64, theta, out);
+}
+
+int gh_tree_force_position(const double* pos, const double* mass, int64_t np, const double* force_pos,
+                           int64_t nf, double eps, double theta, double* out) {
+  if (!force_pos && nf > 0) return set_error(GH_ERR_ARG, "force_pos is NULL");
+  if (nf == 0) return GH_OK;
+  return host_call(HK_TREE, pos, mass, np, force_pos, nf, eps, GH_PREC_FP64, theta, out);
+}
+
+int gh_tree_dev(const double* pos, const double* mass, int64_t np, const double* force_pos, int64_t nf,
+                double eps, double theta, double* acc, void* stream) {
+  clear_error();
+  return tree_force(pos, mass, np, force_pos, nf, eps, theta, acc, (cudaStream_t)stream);
+}
+
 int gh_direct_host(const double* pos, const double* mass, int64_t np, const double* force_pos,
                    int64_t nf, double eps, int precision, double* out) {
   return host_call(HK_DIRECT, pos, mass, np, force_pos, nf, eps, precision, 0.0, out);

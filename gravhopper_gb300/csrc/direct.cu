@@ -235,6 +235,14 @@ int direct_force(const double* pos, const double* mass, int64_t np, const double
   return launch_mixed(ws, (const float4*)ws.src[0].ptr, np, tgt, nt, eps, epi, st);
 }
 
+int drift_prepare_f64(const double* x, const double* v, int64_t n, double dt, double* xh, cudaStream_t st) {
+  if (n == 0) return GH_OK;
+  const int T = 256;
+  drift_prepare_kernel<<<(unsigned)((n + T - 1) / T), T, 0, st>>>(x, v, nullptr, n, dt, nullptr, nullptr, xh);
+  GH_LAUNCH_CHECK();
+  return GH_OK;
+}
+
 int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
                double eps, int precision, double* hist_x, double* hist_v, int64_t stride,
                cudaStream_t st) {

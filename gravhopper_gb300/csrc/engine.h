@@ -16,6 +16,9 @@ int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nst
                double eps, int precision, double* hist_x, double* hist_v, int64_t stride,
                cudaStream_t st);
 
+// First half-drift of a run into an FP64 (N,3) array: xh = x + ((0.5*v)*dt)*F.
+int drift_prepare_f64(const double* x, const double* v, int64_t n, double dt, double* xh, cudaStream_t st);
+
 // Barnes-Hut acceleration in code units (tpos == nullptr: targets are the sources).
 int tree_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt,
                double eps, double theta, double* acc, cudaStream_t st);

@@ -1,17 +1,625 @@
-// Barnes-Hut octree on the GPU (placeholder until the tree kernels land).
+// Barnes-Hut octree on the GPU with the reference's exact cell geometry and
+// opening decisions (gravhopper/_jbgrav.c:360-541, 737-806).
+//
+// Build (every force evaluation):
+//   1. bounding box and root cell with the reference's boxsize rule (_jbgrav.c:747-775);
+//   2. per-particle octant keys: at each level the octant is (x>cx, y>cy, z>cz) and the
+//      child centre is c + (+-0.5*halfsize), the same FP64 recurrence as
+//      gravoct_calc_subnode / gravoct_add_particle (_jbgrav.c:403-428, 453-462).
+//      21 levels per 64-bit word, MSB first, digit = x | y<<1 | z<<2 (the reference's
+//      branch number, _jbgrav.c:441-450), so key order is depth-first order with
+//      children in branch order 0..7.  The number of words grows until no two
+//      particles share a full key (coincident particles end with GH_ERR_DEPTH);
+//   3. stable radix sort of the keys;
+//   4. the node set of the reference's uncompressed octree (every cell that holds a
+//      particle and whose parent holds at least two, single-child chains included)
+//      laid out in depth-first preorder with skip ("next") indices, from the common
+//      prefix lengths of neighbouring keys;
+//   5. monopole pass: leaves take the particle's position and mass exactly
+//      (gravoct_finalize, _jbgrav.c:467-483); internal cells sum their children's
+//      mass and first moment (the reference sums per particle in insertion order, so
+//      the last bits of an internal COM can differ) and divide.
+// Walk: one warp per 32 consecutive targets in key order.  Each lane applies the
+// reference's test "leaf or size/|center - x| < theta" (_jbgrav.c:496-502) to every
+// cell its own traversal reaches; the warp visits the union of those cells in
+// preorder, a lane skipping the subtrees it accepted.  The test is decided in FP32
+// from hi/lo split coordinates with a 1e-4 relative margin; inside the margin it is
+// recomputed with the reference's FP64 operations, so every lane takes exactly the
+// reference's decisions.  Accepted cells contribute (COM - x) m / (r^2 + eps^2)^1.5 in
+// FP64, with the reference's zero for r^2 + eps^2 == 0 (_jbgrav.c:514-520).
+#include <mutex>
+
+#include "direct.cuh"
 #include "engine.h"
-#include "gh_common.cuh"
+#include "sort.cuh"
 
 namespace gh {
 
-int tree_force(const double*, const double*, int64_t, const double*, int64_t, double, double,
-               double*, cudaStream_t) {
-  return set_error(GH_ERR_ARG, "tree force not available in this build");
+constexpr int KEY_LEVELS = 21;
+constexpr int KEY_BITS = 63;
+constexpr int TREE_MIN_WORDS = 2;
+constexpr int TREE_MAX_WORDS = 6;
+constexpr double TREE_MARGIN = 1e-4;
+
+struct TreeRoot {
+  double c[3];
+  double size;
+};
+
+// ---------------------------------------------------------------------------
+// 1. Bounding box and root cell
+// ---------------------------------------------------------------------------
+constexpr int BB_THREADS = 256;
+constexpr int BB_BLOCKS = 304;
+
+__global__ void __launch_bounds__(BB_THREADS)
+    bbox_partial_kernel(const double* __restrict__ pos, int64_t n, double* __restrict__ part) {
+  __shared__ double s_mn[3][BB_THREADS], s_mx[3][BB_THREADS];
+  double mn[3], mx[3];
+  bool have = false;
+  for (int64_t i = (int64_t)blockIdx.x * BB_THREADS + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * BB_THREADS) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      double q = pos[3 * i + k];
+      if (!have) {
+        mn[k] = mx[k] = q;
+      } else {
+        if (q < mn[k]) mn[k] = q;
+        if (q > mx[k]) mx[k] = q;
+      }
+    }
+    have = true;
+  }
+  if (!have) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      mn[k] = __longlong_as_double(0x7ff0000000000000ll);   // +inf
+      mx[k] = __longlong_as_double(0xfff0000000000000ll);   // -inf
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    s_mn[k][threadIdx.x] = mn[k];
+    s_mx[k][threadIdx.x] = mx[k];
+  }
+  __syncthreads();
+  for (int s = BB_THREADS / 2; s > 0; s >>= 1) {
+    if (threadIdx.x < s) {
+#pragma unroll
+      for (int k = 0; k < 3; k++) {
+        double a = s_mn[k][threadIdx.x + s], b = s_mx[k][threadIdx.x + s];
+        if (a < s_mn[k][threadIdx.x]) s_mn[k][threadIdx.x] = a;
+        if (b > s_mx[k][threadIdx.x]) s_mx[k][threadIdx.x] = b;
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      part[6 * blockIdx.x + k] = s_mn[k][0];
+      part[6 * blockIdx.x + 3 + k] = s_mx[k][0];
+    }
+  }
 }
 
-int tree_run(double*, double*, const double*, int64_t, int64_t, double, double, double, double*,
-             double*, int64_t, cudaStream_t) {
-  return set_error(GH_ERR_ARG, "tree force not available in this build");
+// treeforce_workhorse, _jbgrav.c:764-772: boxsize = extent_x + eps, replaced by
+// extent_i + eps when extent_i (without eps) exceeds it; centre = bbox midpoint.
+__global__ void root_kernel(const double* __restrict__ part, int nb, double eps, TreeRoot* __restrict__ root) {
+  if (threadIdx.x || blockIdx.x) return;
+  double mn[3], mx[3];
+  for (int k = 0; k < 3; k++) {
+    mn[k] = part[k];
+    mx[k] = part[3 + k];
+  }
+  for (int b = 1; b < nb; b++)
+    for (int k = 0; k < 3; k++) {
+      double a = part[6 * b + k], c = part[6 * b + 3 + k];
+      if (a < mn[k]) mn[k] = a;
+      if (c > mx[k]) mx[k] = c;
+    }
+  double bs = dadd(dsub(mx[0], mn[0]), eps);
+  for (int k = 1; k < 3; k++)
+    if (dsub(mx[k], mn[k]) > bs) bs = dadd(dsub(mx[k], mn[k]), eps);
+  for (int k = 0; k < 3; k++) root->c[k] = dmul(0.5, dadd(mn[k], mx[k]));
+  root->size = bs;
+}
+
+// ---------------------------------------------------------------------------
+// 2. Octant keys
+// ---------------------------------------------------------------------------
+__global__ void keys_kernel(const double* __restrict__ pos, int64_t n, const TreeRoot* __restrict__ root,
+                            int words, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const double p0 = pos[3 * i], p1 = pos[3 * i + 1], p2 = pos[3 * i + 2];
+  double c0 = root->c[0], c1 = root->c[1], c2 = root->c[2];
+  double hs = dmul(0.5, root->size);
+  for (int w = 0; w < words; w++) {
+    uint64_t k = 0;
+    for (int l = 0; l < KEY_LEVELS; l++) {
+      const double off = dmul(0.5, hs);
+      const unsigned g0 = p0 > c0, g1 = p1 > c1, g2 = p2 > c2;
+      c0 = g0 ? dadd(c0, off) : dsub(c0, off);
+      c1 = g1 ? dadd(c1, off) : dsub(c1, off);
+      c2 = g2 ? dadd(c2, off) : dsub(c2, off);
+      hs = dmul(0.5, hs);
+      k = (k << 3) | (uint64_t)(g0 | (g1 << 1) | (g2 << 2));
+    }
+    keys[(int64_t)w * n + i] = k;
+  }
+  idx[i] = (uint32_t)i;
+}
+
+__device__ __forceinline__ int key_lcp(const uint64_t* __restrict__ keys, int words, int64_t n, int64_t a,
+                                       int64_t b) {
+  for (int w = 0; w < words; w++) {
+    uint64_t x = keys[(int64_t)w * n + a] ^ keys[(int64_t)w * n + b];
+    if (x) return w * KEY_LEVELS + (__clzll((long long)x) - 1) / 3;
+  }
+  return words * KEY_LEVELS;
+}
+
+__device__ __forceinline__ unsigned key_digit(const uint64_t* __restrict__ keys, int64_t n, int64_t i, int level) {
+  const int w = level / KEY_LEVELS, l = level - w * KEY_LEVELS;
+  return (unsigned)((keys[(int64_t)w * n + i] >> (3 * (KEY_LEVELS - 1 - l))) & 7u);
+}
+
+// flags[0]: two particles share a full key; flags[1]: deepest leaf level.
+__global__ void lcp_kernel(const uint64_t* __restrict__ keys, int words, int64_t n, int* __restrict__ lp,
+                           int* __restrict__ flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i > n) return;
+  if (i == 0 || i == n) {
+    lp[i] = -1;
+    return;
+  }
+  int l = key_lcp(keys, words, n, i - 1, i);
+  lp[i] = l;
+  if (l >= words * KEY_LEVELS) atomicOr(&flags[0], 1);
+}
+
+// Leaf level d_i = 1 + max(common prefix with either neighbour); particle i opens
+// the cells at levels lp[i]+1 .. d_i (count d_i - lp[i]).
+__global__ void count_kernel(const int* __restrict__ lp, int64_t n, int* __restrict__ cnt,
+                             int* __restrict__ depth, int* __restrict__ flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int a = lp[i], b = lp[i + 1];
+  const int d = 1 + (a > b ? a : b);
+  depth[i] = d;
+  cnt[i] = d - a;
+  atomicMax(&flags[1], d);
+}
+
+// ---------------------------------------------------------------------------
+// 4. Nodes in preorder
+// ---------------------------------------------------------------------------
+struct NodeArrays {
+  float4* A;     // (cx_hi, cy_hi, cz_hi, size^2)        FP32 opening prefilter
+  float4* L;     // (cx_lo, cy_lo, cz_lo, next as bits)   FP32 residuals + skip index
+  dvec4* C;      // (cx, cy, cz, size)                    exact opening test
+  dvec4* M;      // (comx, comy, comz, mass)              interaction
+  dvec4* F;      // (first moment x, y, z, mass)          build only
+  int* first;    // first particle (sorted position)
+  int* level;
+};
+
+__device__ __forceinline__ float f32_hi(double v) { return (float)v; }
+__device__ __forceinline__ float f32_lo(double v, float hi) { return (float)(v - (double)hi); }
+
+__global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
+                             const int* __restrict__ lp, const int* __restrict__ depth,
+                             const int* __restrict__ base, const TreeRoot* __restrict__ root, NodeArrays na,
+                             int nnodes) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int lo = lp[i] + 1, d = depth[i];
+  const int k0 = base[i];
+  double c[3] = {root->c[0], root->c[1], root->c[2]};
+  double size = root->size;
+  for (int L = 0; L <= d; L++) {
+    if (L >= lo) {
+      const int k = k0 + (L - lo);
+      int64_t end;
+      if (L == d) {
+        end = i + 1;
+      } else {
+        // last particle sharing the first L digits with i
+        int64_t a = i, b = n - 1;
+        while (a < b) {
+          int64_t mid = (a + b + 1) >> 1;
+          if (key_lcp(keys, words, n, i, mid) >= L)
+            a = mid;
+          else
+            b = mid - 1;
+        }
+        end = a + 1;
+      }
+      const int next = end < n ? base[end] : nnodes;
+      float4 A, Lo;
+      A.x = f32_hi(c[0]);
+      A.y = f32_hi(c[1]);
+      A.z = f32_hi(c[2]);
+      A.w = (float)dmul(size, size);
+      Lo.x = f32_lo(c[0], A.x);
+      Lo.y = f32_lo(c[1], A.y);
+      Lo.z = f32_lo(c[2], A.z);
+      Lo.w = __int_as_float(next);
+      na.A[k] = A;
+      na.L[k] = Lo;
+      na.C[k] = make_dvec4(c[0], c[1], c[2], size);
+      na.first[k] = (int)i;
+      na.level[k] = L;
+    }
+    if (L < d) {
+      const unsigned g = key_digit(keys, n, i, L);
+      const double hs = dmul(0.5, size);
+      const double off = dmul(0.5, hs);
+#pragma unroll
+      for (int q = 0; q < 3; q++) c[q] = ((g >> q) & 1u) ? dadd(c[q], off) : dsub(c[q], off);
+      size = hs;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// 5. Monopole pass, deepest level first
+// ---------------------------------------------------------------------------
+__global__ void level_hist_kernel(const int* __restrict__ level, int nnodes, int* __restrict__ hist) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nnodes) atomicAdd(&hist[level[k]], 1);
+}
+
+// hist (levels+1 entries) -> off (exclusive prefix) and cursor (= off)
+__global__ void level_scan_kernel(const int* __restrict__ hist, int levels, int* __restrict__ off,
+                                  int* __restrict__ cursor) {
+  if (threadIdx.x || blockIdx.x) return;
+  int s = 0;
+  for (int l = 0; l < levels; l++) {
+    off[l] = s;
+    cursor[l] = s;
+    s += hist[l];
+  }
+  off[levels] = s;
+}
+
+__global__ void level_scatter_kernel(const int* __restrict__ level, int nnodes, int* __restrict__ cursor,
+                                     int* __restrict__ bucket) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < nnodes) bucket[atomicAdd(&cursor[level[k]], 1)] = k;
+}
+
+__device__ __forceinline__ int node_next(const float4* __restrict__ L, int k) { return __float_as_int(L[k].w); }
+
+__global__ void com_leaf_kernel(NodeArrays na, int nnodes, const uint32_t* __restrict__ perm,
+                                const double* __restrict__ pos, const double* __restrict__ mass) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= nnodes || node_next(na.L, k) != k + 1) return;
+  const int64_t p = perm[na.first[k]];
+  const double m = mass[p];
+  const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
+  na.M[k] = make_dvec4(x, y, z, m);
+  na.F[k] = make_dvec4(dmul(m, x), dmul(m, y), dmul(m, z), m);
+}
+
+__global__ void com_level_kernel(NodeArrays na, const int* __restrict__ bucket, const int* __restrict__ off,
+                                 int level) {
+  const int b0 = off[level], b1 = off[level + 1];
+  for (int t = b0 + blockIdx.x * blockDim.x + threadIdx.x; t < b1; t += gridDim.x * blockDim.x) {
+    const int k = bucket[t];
+    const int nx = node_next(na.L, k);
+    if (nx == k + 1) continue;  // leaf
+    double fx = 0.0, fy = 0.0, fz = 0.0, m = 0.0;
+    for (int c = k + 1; c < nx; c = node_next(na.L, c)) {
+      const dvec4 f = na.F[c];
+      fx = dadd(fx, f.x);
+      fy = dadd(fy, f.y);
+      fz = dadd(fz, f.z);
+      m = dadd(m, f.w);
+    }
+    na.F[k] = make_dvec4(fx, fy, fz, m);
+    na.M[k] = make_dvec4(ddiv(fx, m), ddiv(fy, m), ddiv(fz, m), m);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Walk
+// ---------------------------------------------------------------------------
+constexpr int TW_THREADS = 128;
+
+__device__ __forceinline__ double rsqrt_f64(double s) {
+  double y;
+  asm("rsqrt.approx.f64 %0, %1;" : "=d"(y) : "d"(s));
+  // two Newton steps: y <- y + 0.5 y (1 - s y^2)
+#pragma unroll
+  for (int it = 0; it < 2; it++) {
+    double e = fma(-s * y, y, 1.0);
+    y = fma(0.5 * y, e, y);
+  }
+  return y;
+}
+
+template <bool GUARD, class Epi>
+__global__ void __launch_bounds__(TW_THREADS)
+    tree_walk_kernel(const float4* __restrict__ nA, const float4* __restrict__ nL, const dvec4* __restrict__ nC,
+                     const dvec4* __restrict__ nM, int nnodes, const double* __restrict__ tpos,
+                     const uint32_t* __restrict__ order, int64_t nt, double eps2, double theta, float th2_lo,
+                     float th2_hi, Epi epi) {
+  const int64_t slot = (int64_t)blockIdx.x * TW_THREADS + threadIdx.x;
+  const bool valid = slot < nt;
+  const int64_t t = valid ? (order ? (int64_t)order[slot] : slot) : 0;
+  double p0 = 0.0, p1 = 0.0, p2 = 0.0;
+  if (valid) {
+    p0 = tpos[3 * t];
+    p1 = tpos[3 * t + 1];
+    p2 = tpos[3 * t + 2];
+  }
+  const float h0 = (float)p0, h1 = (float)p1, h2 = (float)p2;
+  const float l0 = f32_lo(p0, h0), l1 = f32_lo(p1, h1), l2 = f32_lo(p2, h2);
+  // d^2 below this needs the exact test: FP32 differences lose too much relative to |x|
+  const float near2 = 1e-18f * (h0 * h0 + h1 * h1 + h2 * h2);
+  double ax = 0.0, ay = 0.0, az = 0.0;
+  int skip = valid ? 0 : 0x7fffffff;
+  int node = __reduce_min_sync(0xffffffffu, skip);
+  while (node < nnodes) {
+    int lane_next = skip;
+    if (node >= skip) {
+      const float4 A = nA[node];
+      const float4 Lo = nL[node];
+      const int nx = __float_as_int(Lo.w);
+      bool accept = (nx == node + 1);  // leaf
+      if (!accept) {
+        const float dx = (A.x - h0) + (Lo.x - l0);
+        const float dy = (A.y - h1) + (Lo.y - l1);
+        const float dz = (A.z - h2) + (Lo.z - l2);
+        const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
+        const float s2 = A.w;
+        const bool usable = d2 > near2 && d2 > 1e-30f && d2 < 1e30f && s2 > 1e-30f;
+        if (usable && s2 < th2_lo * d2) {
+          accept = true;
+        } else if (usable && s2 > th2_hi * d2) {
+          accept = false;
+        } else {
+          // gravoct_calc_accel opening test with the reference's FP64 operations
+          const dvec4 C = nC[node];
+          const double e0 = dsub(C.x, p0), e1 = dsub(C.y, p1), e2 = dsub(C.z, p2);
+          double nd = dmul(e0, e0);
+          nd = dadd(nd, dmul(e1, e1));
+          nd = dadd(nd, dmul(e2, e2));
+          accept = ddiv(C.w, dsqrt(nd)) < theta;
+        }
+      }
+      if (accept) {
+        const dvec4 M = nM[node];
+        const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
+        const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+        if (!GUARD || s != 0.0) {
+          const double y = rsqrt_f64(s);
+          const double f = M.w * (y * (y * y));
+          ax = fma(f, dx, ax);
+          ay = fma(f, dy, ay);
+          az = fma(f, dz, az);
+        }
+        skip = nx;
+        lane_next = nx;
+      } else {
+        lane_next = node + 1;
+      }
+    }
+    node = __reduce_min_sync(0xffffffffu, lane_next);
+  }
+  if (valid) epi(t, ax, ay, az);
+}
+
+// ---------------------------------------------------------------------------
+// Workspace and host driver
+// ---------------------------------------------------------------------------
+struct TreeWS {
+  Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
+  Buffer nA, nL, nC, nM, nF, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
+  int* host_flags = nullptr;  // pinned: tie, maxdepth, nnodes
+  int words = TREE_MIN_WORDS;
+};
+static TreeWS g_tree[64];
+static std::recursive_mutex g_tree_mu;
+
+static NodeArrays node_arrays(TreeWS& ws) {
+  NodeArrays na;
+  na.A = (float4*)ws.nA.ptr;
+  na.L = (float4*)ws.nL.ptr;
+  na.C = (dvec4*)ws.nC.ptr;
+  na.M = (dvec4*)ws.nM.ptr;
+  na.F = (dvec4*)ws.nF.ptr;
+  na.first = (int*)ws.first.ptr;
+  na.level = (int*)ws.level.ptr;
+  return na;
+}
+
+struct BuiltTree {
+  int nnodes = 0;
+  int maxdepth = 0;
+};
+
+static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t n, double eps,
+                      cudaStream_t st, BuiltTree* out) {
+  // int32 node indices: at most 127 cells per particle
+  if (n > (1LL << 24)) return set_error(GH_ERR_ARG, "tree: at most 16777216 particles (got %lld)", (long long)n);
+  if (!ws.host_flags) GH_CUDA_TRY(cudaMallocHost((void**)&ws.host_flags, 4 * sizeof(int)));
+  const int T = 256;
+  // 1. root cell
+  GH_TRY(ensure(ws.part, BB_BLOCKS * 6 * sizeof(double)));
+  GH_TRY(ensure(ws.root, sizeof(TreeRoot)));
+  int nb = (int)((n + BB_THREADS - 1) / BB_THREADS);
+  if (nb > BB_BLOCKS) nb = BB_BLOCKS;
+  bbox_partial_kernel<<<nb, BB_THREADS, 0, st>>>(pos, n, (double*)ws.part.ptr);
+  GH_LAUNCH_CHECK();
+  root_kernel<<<1, 32, 0, st>>>((const double*)ws.part.ptr, nb, eps, (TreeRoot*)ws.root.ptr);
+  GH_LAUNCH_CHECK();
+  const TreeRoot* root = (const TreeRoot*)ws.root.ptr;
+  const unsigned gn = (unsigned)((n + T - 1) / T), gn1 = (unsigned)((n + 1 + T - 1) / T);
+  GH_TRY(ensure(ws.lp, (n + 1) * sizeof(int)));
+  GH_TRY(ensure(ws.cnt, n * sizeof(int)));
+  GH_TRY(ensure(ws.depth, n * sizeof(int)));
+  GH_TRY(ensure(ws.base, (n + 1) * sizeof(int)));
+  GH_TRY(ensure(ws.scan, scan_scratch_ints(n) * sizeof(int)));
+  GH_TRY(ensure(ws.flags, 4 * sizeof(int)));
+  GH_TRY(ensure(ws.idx, n * sizeof(uint32_t)));
+  GH_TRY(ensure(ws.idx_tmp, n * sizeof(uint32_t)));
+  GH_TRY(ensure(ws.rs, radix_scratch_words(n) * sizeof(uint32_t)));
+  // 2-3. keys, sort, prefix structure; widen the keys while particles tie
+  for (;;) {
+    const int words = ws.words;
+    GH_TRY(ensure(ws.keys, (size_t)words * n * sizeof(uint64_t)));
+    GH_TRY(ensure(ws.keys_tmp, (size_t)words * n * sizeof(uint64_t)));
+    uint64_t* keys = (uint64_t*)ws.keys.ptr;
+    keys_kernel<<<gn, T, 0, st>>>(pos, n, root, words, keys, (uint32_t*)ws.idx.ptr);
+    GH_LAUNCH_CHECK();
+    GH_TRY(radix_sort_keys(keys, (uint32_t*)ws.idx.ptr, (uint64_t*)ws.keys_tmp.ptr, (uint32_t*)ws.idx_tmp.ptr,
+                           words, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
+    GH_CUDA_TRY(cudaMemsetAsync(ws.flags.ptr, 0, 4 * sizeof(int), st));
+    lcp_kernel<<<gn1, T, 0, st>>>(keys, words, n, (int*)ws.lp.ptr, (int*)ws.flags.ptr);
+    GH_LAUNCH_CHECK();
+    count_kernel<<<gn, T, 0, st>>>((const int*)ws.lp.ptr, n, (int*)ws.cnt.ptr, (int*)ws.depth.ptr,
+                                   (int*)ws.flags.ptr);
+    GH_LAUNCH_CHECK();
+    GH_TRY(exclusive_scan_i32((const int*)ws.cnt.ptr, (int*)ws.base.ptr, n, (int*)ws.scan.ptr, st));
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 2, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
+                                st));
+    GH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!ws.host_flags[0]) break;
+    if (ws.words >= TREE_MAX_WORDS)
+      return set_error(GH_ERR_DEPTH,
+                       "tree: particles share their first %d octree levels (coincident positions?)",
+                       TREE_MAX_WORDS * KEY_LEVELS);
+    ws.words++;
+  }
+  const int words = ws.words;
+  const int maxdepth = ws.host_flags[1];
+  const int nnodes = ws.host_flags[2];
+  // 4. nodes
+  GH_TRY(ensure(ws.nA, (size_t)nnodes * sizeof(float4)));
+  GH_TRY(ensure(ws.nL, (size_t)nnodes * sizeof(float4)));
+  GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));
+  GH_TRY(ensure(ws.nM, (size_t)nnodes * sizeof(dvec4)));
+  GH_TRY(ensure(ws.nF, (size_t)nnodes * sizeof(dvec4)));
+  GH_TRY(ensure(ws.first, (size_t)nnodes * sizeof(int)));
+  GH_TRY(ensure(ws.level, (size_t)nnodes * sizeof(int)));
+  NodeArrays na = node_arrays(ws);
+  nodes_kernel<<<gn, T, 0, st>>>((const uint64_t*)ws.keys.ptr, words, n, (const int*)ws.lp.ptr,
+                                 (const int*)ws.depth.ptr, (const int*)ws.base.ptr, root, na, nnodes);
+  GH_LAUNCH_CHECK();
+  // 5. monopoles, by level
+  const int levels = maxdepth + 1;
+  GH_TRY(ensure(ws.lvl_hist, (levels + 1) * sizeof(int)));
+  GH_TRY(ensure(ws.lvl_off, (levels + 1) * sizeof(int)));
+  GH_TRY(ensure(ws.lvl_cursor, (levels + 1) * sizeof(int)));
+  GH_TRY(ensure(ws.bucket, (size_t)nnodes * sizeof(int)));
+  GH_CUDA_TRY(cudaMemsetAsync(ws.lvl_hist.ptr, 0, (levels + 1) * sizeof(int), st));
+  const unsigned gk = (unsigned)((nnodes + T - 1) / T);
+  level_hist_kernel<<<gk, T, 0, st>>>(na.level, nnodes, (int*)ws.lvl_hist.ptr);
+  GH_LAUNCH_CHECK();
+  level_scan_kernel<<<1, 32, 0, st>>>((const int*)ws.lvl_hist.ptr, levels, (int*)ws.lvl_off.ptr,
+                                      (int*)ws.lvl_cursor.ptr);
+  GH_LAUNCH_CHECK();
+  level_scatter_kernel<<<gk, T, 0, st>>>(na.level, nnodes, (int*)ws.lvl_cursor.ptr, (int*)ws.bucket.ptr);
+  GH_LAUNCH_CHECK();
+  com_leaf_kernel<<<gk, T, 0, st>>>(na, nnodes, (const uint32_t*)ws.idx.ptr, pos, mass);
+  GH_LAUNCH_CHECK();
+  for (int l = maxdepth - 1; l >= 0; l--) {
+    com_level_kernel<<<2 * 152, T, 0, st>>>(na, (const int*)ws.bucket.ptr, (const int*)ws.lvl_off.ptr, l);
+    GH_LAUNCH_CHECK();
+  }
+  out->nnodes = nnodes;
+  out->maxdepth = maxdepth;
+  return GH_OK;
+}
+
+template <class Epi>
+static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const uint32_t* order, int64_t nt,
+                     double eps, double theta, const Epi& epi, cudaStream_t st) {
+  if (nt == 0) return GH_OK;
+  const double eps2 = eps * eps;
+  float lo = -1.f, hi = -1.f;  // theta <= 0 or NaN: never open by the prefilter, never accept
+  if (theta > 0.0) {
+    lo = (float)(theta * theta * (1.0 - TREE_MARGIN));
+    hi = (float)(theta * theta * (1.0 + TREE_MARGIN));
+  }
+  const unsigned blocks = (unsigned)((nt + TW_THREADS - 1) / TW_THREADS);
+  NodeArrays na = node_arrays(ws);
+  prof_begin(st);
+  if (eps2 == 0.0)
+    tree_walk_kernel<true, Epi><<<blocks, TW_THREADS, 0, st>>>(na.A, na.L, na.C, na.M, bt.nnodes, tpos, order, nt,
+                                                               eps2, theta, lo, hi, epi);
+  else
+    tree_walk_kernel<false, Epi><<<blocks, TW_THREADS, 0, st>>>(na.A, na.L, na.C, na.M, bt.nnodes, tpos, order,
+                                                                nt, eps2, theta, lo, hi, epi);
+  prof_end(st);
+  GH_LAUNCH_CHECK();
+  return GH_OK;
+}
+
+static int check_tree_args(int64_t np, int64_t nt, double eps) {
+  if (np < 0 || nt < 0) return set_error(GH_ERR_ARG, "negative particle count");
+  if (!(eps >= 0.0)) return set_error(GH_ERR_ARG, "eps must be >= 0 (got %g)", eps);
+  return GH_OK;
+}
+
+int tree_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt, double eps,
+               double theta, double* acc, cudaStream_t st) {
+  GH_TRY(check_tree_args(np, nt, eps));
+  const bool self = (tpos == nullptr);
+  if (self) nt = np;
+  if (nt == 0) return GH_OK;
+  if (np == 0) {
+    GH_CUDA_TRY(cudaMemsetAsync(acc, 0, (size_t)nt * 3 * sizeof(double), st));
+    return GH_OK;
+  }
+  std::lock_guard<std::recursive_mutex> lk(g_tree_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  TreeWS& ws = g_tree[di.device];
+  BuiltTree bt;
+  GH_TRY(tree_build(ws, pos, mass, np, eps, st, &bt));
+  EpiStore epi{acc};
+  if (self) return tree_walk(ws, bt, pos, (const uint32_t*)ws.idx.ptr, np, eps, theta, epi, st);
+  return tree_walk(ws, bt, tpos, nullptr, nt, eps, theta, epi, st);
+}
+
+int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt, double eps,
+             double theta, double* hist_x, double* hist_v, int64_t stride, cudaStream_t st) {
+  GH_TRY(check_tree_args(np, 0, eps));
+  std::lock_guard<std::recursive_mutex> lk(g_tree_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  TreeWS& ws = g_tree[di.device];
+  GH_TRY(ensure(ws.xh[0], (size_t)np * 3 * sizeof(double)));
+  GH_TRY(ensure(ws.xh[1], (size_t)np * 3 * sizeof(double)));
+  GH_TRY(drift_prepare_f64(x, v, np, dt, (double*)ws.xh[0].ptr, st));
+  for (int64_t s = 0; s < nsteps; s++) {
+    const int cur = (int)(s & 1), nxt = cur ^ 1;
+    const double* xh = (const double*)ws.xh[cur].ptr;
+    BuiltTree bt;
+    GH_TRY(tree_build(ws, xh, mass, np, eps, st, &bt));
+    EpiDKD epi;
+    epi.x = x;
+    epi.v = v;
+    epi.mass = mass;
+    epi.dt = dt;
+    epi.src_next = nullptr;
+    epi.origin = nullptr;
+    epi.xh_next = (double*)ws.xh[nxt].ptr;
+    epi.hist_x = epi.hist_v = nullptr;
+    if (hist_x && stride > 0 && (s + 1) % stride == 0) {
+      const int64_t slot = (s + 1) / stride - 1;
+      epi.hist_x = hist_x + slot * np * 3;
+      epi.hist_v = hist_v + slot * np * 3;
+    }
+    GH_TRY(tree_walk(ws, bt, xh, (const uint32_t*)ws.idx.ptr, np, eps, theta, epi, st));
+  }
+  return GH_OK;
 }
 
 }  // namespace gh

@@ -63,6 +63,19 @@ int gh_direct_summation(const double* pos, const double* mass, int64_t np, doubl
 int gh_direct_summation_position(const double* pos, const double* mass, int64_t np,
                                  const double* force_pos, int64_t nf, double eps, double* out);
 
+/* Replaces _jbgrav.tree_force(pos, mass, eps, theta), gravhopper/_jbgrav.c:564-630 and
+ * treeforce_workhorse :737-806.  Barnes-Hut octree with the reference's cells,
+ * centres and opening test (leaf, or size/|center - x| < theta); monopoles; FP64.
+ * Returns GH_ERR_DEPTH for particles that share position to 126 octree levels
+ * (the reference recurses without bound on coincident particles). */
+int gh_tree_force(const double* pos, const double* mass, int64_t np, double eps, double theta,
+                  double* out);
+
+/* Replaces _jbgrav.tree_force_position(pos, mass, force_pos, eps, theta),
+ * gravhopper/_jbgrav.c:634-727.  np == 0 gives zeros. */
+int gh_tree_force_position(const double* pos, const double* mass, int64_t np, const double* force_pos,
+                           int64_t nf, double eps, double theta, double* out);
+
 /* Direct sum with a precision choice (GH_PREC_*).  force_pos == NULL: targets are
  * the particles themselves and the self term is skipped (direct_summation). */
 int gh_direct_host(const double* pos, const double* mass, int64_t np, const double* force_pos,
@@ -74,6 +87,10 @@ int gh_direct_host(const double* pos, const double* mass, int64_t np, const doub
  * force_pos == NULL (self term skipped). */
 int gh_direct_dev(const double* pos, const double* mass, int64_t np, const double* force_pos,
                   int64_t nf, double eps, int precision, double* acc, void* stream);
+
+/* Barnes-Hut acceleration (code units) into acc (nf,3), or (np,3) when force_pos == NULL. */
+int gh_tree_dev(const double* pos, const double* mass, int64_t np, const double* force_pos, int64_t nf,
+                double eps, double theta, double* acc, void* stream);
 
 /* Advances (pos, vel) in place by nsteps drift-kick-drift leapfrog steps
  * (Simulation.perform_timestep, gravhopper/gravhopper.py:405-416): pos [kpc],
