@@ -72,6 +72,10 @@ SIGNATURES = {
     "gh_run_dkd": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _int, _dbl, _vp, _vp, _i64,
                           _vp]),
     "gh_measure_fma_peaks": (_int, [_vp, _vp, _vp]),
+    "gh_ensemble_run": (_int, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _i64, _int, _int, _vp]),
+    "gh_ensemble_num_configs": (_int, []),
+    "gh_direct_set_shape": (_int, [_int]),
+    "gh_direct_num_shapes": (_int, []),
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),
 }

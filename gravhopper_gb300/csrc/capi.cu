@@ -2,6 +2,7 @@
 // device-pointer, stream-ordered calls.
 #include <mutex>
 
+#include "direct.cuh"
 #include "engine.h"
 #include "gh_common.cuh"
 
@@ -143,5 +144,22 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
                       hist_stride, st);
   return tree_run(pos, vel, mass, np, nsteps, dt, eps, theta, hist_pos, hist_vel, hist_stride, st);
 }
+
+int gh_ensemble_run(double* pos, double* vel, const double* mass, const int64_t* offsets, int64_t nsys,
+                    const double* eps, const double* dt, int64_t nsteps, int tile_config, int use_graph,
+                    void* stream) {
+  clear_error();
+  return ensemble_run(pos, vel, mass, offsets, nsys, eps, dt, nsteps, tile_config, use_graph,
+                      (cudaStream_t)stream);
+}
+
+int gh_ensemble_num_configs(void) { return ensemble_num_configs(); }
+
+int gh_direct_set_shape(int shape) {
+  clear_error();
+  return set_mixed_shape(shape);
+}
+
+int gh_direct_num_shapes(void) { return kNumMixedShapes; }
 
 }  // extern "C"

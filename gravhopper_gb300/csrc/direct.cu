@@ -6,7 +6,6 @@
 
 namespace gh {
 
-static_assert(MX_JT == MX_THREADS, "one source per thread per chunk fill");
 
 // ---------------------------------------------------------------------------
 // Small kernels: mass-weighted centre (deterministic two-pass), conversion to
@@ -99,30 +98,70 @@ struct DirectWS {
 static DirectWS g_ws[64];
 static std::recursive_mutex g_mu;
 
-static int mixed_grid_cap(int num_sms, bool guard) {
-  static int occ[2] = {0, 0};
-  int& o = occ[guard ? 1 : 0];
+// Shape of the mixed kernel used by this library (index into kMixedShapes).
+static int g_mixed_shape = 0;
+
+template <bool G, int T, int P, int B, class Epi>
+static int launch_shape(const StreamK& sk, const float4* src, int64_t np, const float4* tgt, int64_t nt,
+                        float eps2, float* partials, int* counters, const Epi& epi, cudaStream_t st) {
+  direct_mixed_kernel<G, T, P, B, Epi><<<(unsigned)sk.grid, T, 0, st>>>(src, np, tgt, nt, eps2, sk, partials,
+                                                                        counters, epi);
+  return GH_OK;
+}
+
+template <bool G, int T, int P, int B>
+static int occupancy_shape() {
+  int o = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<G, T, P, B, EpiStore>, T, 0) !=
+          cudaSuccess ||
+      o < 1)
+    o = 1;
+  return o;
+}
+
+template <bool G, class Epi>
+static int dispatch_shape(int shape, const StreamK& sk, const float4* src, int64_t np, const float4* tgt,
+                          int64_t nt, float eps2, float* partials, int* counters, const Epi& epi,
+                          cudaStream_t st) {
+  switch (shape) {
+    case 0: return launch_shape<G, 256, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 1: return launch_shape<G, 256, 4, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 2: return launch_shape<G, 128, 4, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 3: return launch_shape<G, 128, 2, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    default: return launch_shape<G, 512, 2, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+  }
+}
+
+static int mixed_grid_cap(int num_sms, int shape, bool guard) {
+  static int occ[2][kNumMixedShapes] = {};
+  int& o = occ[guard ? 1 : 0][shape];
   if (o == 0) {
-    cudaError_t e;
-    if (guard)
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<true, EpiStore>,
-                                                        MX_THREADS, 0);
-    else
-      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<false, EpiStore>,
-                                                        MX_THREADS, 0);
-    if (e != cudaSuccess || o < 1) o = 1;
+    switch (shape) {
+      case 0: o = guard ? occupancy_shape<true, 256, 2, 2>() : occupancy_shape<false, 256, 2, 2>(); break;
+      case 1: o = guard ? occupancy_shape<true, 256, 4, 1>() : occupancy_shape<false, 256, 4, 1>(); break;
+      case 2: o = guard ? occupancy_shape<true, 128, 4, 2>() : occupancy_shape<false, 128, 4, 2>(); break;
+      case 3: o = guard ? occupancy_shape<true, 128, 2, 4>() : occupancy_shape<false, 128, 2, 4>(); break;
+      default: o = guard ? occupancy_shape<true, 512, 2, 1>() : occupancy_shape<false, 512, 2, 1>(); break;
+    }
   }
   return o * num_sms;
 }
 
-StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap) {
+StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap, int tile, int jt) {
   StreamK s;
-  s.n_tiles = (nt + MX_TILE - 1) / MX_TILE;
-  s.chunks = (np + MX_JT - 1) / MX_JT;
+  s.n_tiles = (nt + tile - 1) / tile;
+  s.chunks = (np + jt - 1) / jt;
   s.units = s.n_tiles * s.chunks;
   s.grid = s.units < grid_cap ? s.units : grid_cap;
   if (s.grid < 1) s.grid = 1;
   return s;
+}
+
+int set_mixed_shape(int shape) {
+  if (shape < 0) shape = 0;
+  if (shape >= kNumMixedShapes) return set_error(GH_ERR_ARG, "mixed shape %d out of range", shape);
+  g_mixed_shape = shape;
+  return GH_OK;
 }
 
 // Mass-weighted centre of (pos, mass) into ws.origin (3 doubles).
@@ -140,8 +179,8 @@ static int compute_origin(DirectWS& ws, const double* pos, const double* mass, i
   return GH_OK;
 }
 
-static int ensure_streamk(DirectWS& ws, const StreamK& sk, cudaStream_t st) {
-  GH_TRY(ensure(ws.partials, (size_t)(2 * sk.grid * MX_SLOT_FLOATS) * sizeof(float)));
+static int ensure_streamk(DirectWS& ws, const StreamK& sk, int64_t slot_floats, cudaStream_t st) {
+  GH_TRY(ensure(ws.partials, (size_t)(2 * sk.grid * slot_floats) * sizeof(float)));
   size_t cbytes = (size_t)sk.n_tiles * sizeof(int);
   if (ws.counters.bytes < cbytes || ws.counters_zeroed < cbytes) {
     GH_TRY(ensure(ws.counters, cbytes));
@@ -158,16 +197,19 @@ static int launch_mixed(DirectWS& ws, const float4* src, int64_t np, const float
   GH_TRY(device_info(&di));
   const float eps2 = (float)(eps * eps);
   const bool guard = !(eps2 > 0.f);
-  StreamK sk = mixed_plan(np, nt, mixed_grid_cap(di.num_sms, guard));
+  const int shape = g_mixed_shape;
+  const MixedShape ms = kMixedShapes[shape];
+  StreamK sk = mixed_plan(np, nt, mixed_grid_cap(di.num_sms, shape, guard), ms.threads * 2 * ms.packs,
+                          ms.threads);
   if (sk.units == 0) return GH_OK;
-  GH_TRY(ensure_streamk(ws, sk, st));
+  GH_TRY(ensure_streamk(ws, sk, mixed_slot_floats(ms.threads, ms.packs), st));
+  float* partials = (float*)ws.partials.ptr;
+  int* counters = (int*)ws.counters.ptr;
   prof_begin(st);
   if (guard)
-    direct_mixed_kernel<true, Epi><<<(unsigned)sk.grid, MX_THREADS, 0, st>>>(
-        src, np, tgt, nt, eps2, sk, (float*)ws.partials.ptr, (int*)ws.counters.ptr, epi);
+    dispatch_shape<true>(shape, sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
   else
-    direct_mixed_kernel<false, Epi><<<(unsigned)sk.grid, MX_THREADS, 0, st>>>(
-        src, np, tgt, nt, eps2, sk, (float*)ws.partials.ptr, (int*)ws.counters.ptr, epi);
+    dispatch_shape<false>(shape, sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
   prof_end(st);
   GH_LAUNCH_CHECK();
   return GH_OK;

@@ -197,11 +197,13 @@ __global__ void __launch_bounds__(F64_THREADS)
 // the CTA that finishes last (per-tile counter) combines them in CTA order, so
 // the result does not depend on timing, and runs the epilogue.
 // ---------------------------------------------------------------------------
-constexpr int MX_THREADS = 256;
-constexpr int MX_P = 2;                      // f32x2 packs per thread
-constexpr int MX_R = 2 * MX_P;               // targets per thread
-constexpr int MX_TILE = MX_THREADS * MX_R;   // targets per tile
-constexpr int MX_JT = 256;                   // sources per shared-memory chunk
+// Tile shapes of the mixed kernel: THREADS per CTA (also the sources per
+// shared-memory chunk), P f32x2 packs (2P targets) per thread, MINB CTAs per SM.
+struct MixedShape {
+  int threads, packs, minb;
+};
+constexpr MixedShape kMixedShapes[] = {{256, 2, 2}, {256, 4, 1}, {128, 4, 2}, {128, 2, 4}, {512, 2, 1}};
+constexpr int kNumMixedShapes = (int)(sizeof(kMixedShapes) / sizeof(kMixedShapes[0]));
 
 struct StreamK {
   int64_t n_tiles;
@@ -218,17 +220,77 @@ __host__ __device__ __forceinline__ int64_t sk_owner(const StreamK& s, int64_t u
   return ((u + 1) * s.grid + s.units - 1) / s.units - 1;
 }
 
-// Per-CTA scratch for split tiles: 2 slots (first and last tile of its range),
-// each 6 floats (hi/lo for x, y, z) per target.
-constexpr int64_t MX_SLOT_FLOATS = (int64_t)6 * MX_TILE;
+// One shared-memory chunk of JT sources against P packed target pairs: FP32 pair
+// forces summed into a per-chunk partial, then folded into the (h, l) two-sum
+// accumulator.  `tile` holds each source duplicated per lane: (x,x,y,y), (z,z,m,m).
+// Per pair: 3 sub, 3 fma (r^2 + eps^2), 1 MUFU rsqrt, 3 mul, 3 fma.
+template <bool GUARD, int P, int JT>
+__device__ __forceinline__ void mixed_chunk(const float4* __restrict__ tile, const f2* tx, const f2* ty,
+                                            const f2* tz, f2 E2, f2* hx, f2* hy, f2* hz, f2* lx, f2* ly,
+                                            f2* lz) {
+  f2 px[P], py[P], pz[P];
+#pragma unroll
+  for (int p = 0; p < P; p++) px[p] = py[p] = pz[p] = 0ull;
+#pragma unroll 4
+  for (int k = 0; k < JT; k++) {
+    const float4 a = tile[2 * k + 0];
+    const float4 b = tile[2 * k + 1];
+    const f2 X = f2make(a.x, a.y), Y = f2make(a.z, a.w);
+    const f2 Z = f2make(b.x, b.y), M = f2make(b.z, b.w);
+#pragma unroll
+    for (int p = 0; p < P; p++) {
+      f2 dx = f2sub(X, tx[p]);
+      f2 dy = f2sub(Y, ty[p]);
+      f2 dz = f2sub(Z, tz[p]);
+      f2 r2 = f2fma(dx, dx, E2);
+      r2 = f2fma(dy, dy, r2);
+      r2 = f2fma(dz, dz, r2);
+      float r2a, r2b;
+      f2split(r2, r2a, r2b);
+      float ia = rsqrt_approx(r2a), ib = rsqrt_approx(r2b);
+      if (GUARD) {
+        ia = r2a > 0.f ? ia : 0.f;
+        ib = r2b > 0.f ? ib : 0.f;
+      }
+      f2 ri = f2make(ia, ib);
+      f2 ri2 = f2mul(ri, ri);
+      f2 mri = f2mul(M, ri);
+      f2 sc = f2mul(mri, ri2);
+      px[p] = f2fma(sc, dx, px[p]);
+      py[p] = f2fma(sc, dy, py[p]);
+      pz[p] = f2fma(sc, dz, pz[p]);
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < P; p++) {
+    f2 s, e;
+    f2two_sum(hx[p], px[p], s, e);
+    hx[p] = s;
+    lx[p] = f2add(lx[p], e);
+    f2two_sum(hy[p], py[p], s, e);
+    hy[p] = s;
+    ly[p] = f2add(ly[p], e);
+    f2two_sum(hz[p], pz[p], s, e);
+    hz[p] = s;
+    lz[p] = f2add(lz[p], e);
+  }
+}
 
-template <bool GUARD, class Epi>
-__global__ void __launch_bounds__(MX_THREADS, 2)
+// Per-CTA scratch for split tiles: 2 slots (first and last tile of its range),
+// each 6 floats (hi/lo for x, y, z) per target of a tile.
+__host__ __device__ constexpr int64_t mixed_slot_floats(int threads, int packs) {
+  return (int64_t)6 * threads * 2 * packs;
+}
+
+template <bool GUARD, int THREADS, int P, int MINB, class Epi>
+__global__ void __launch_bounds__(THREADS, MINB)
     direct_mixed_kernel(const float4* __restrict__ src, int64_t np, const float4* __restrict__ tgt,
                         int64_t nt, float eps2, StreamK sk, float* __restrict__ partials,
                         int* __restrict__ counters, Epi epi) {
+  constexpr int R = 2 * P, TILE = THREADS * R, JT = THREADS;
+  constexpr int64_t SLOT = mixed_slot_floats(THREADS, P);
   // Sources duplicated per lane pair: (x,x,y,y) and (z,z,m,m).
-  __shared__ __align__(16) float4 tile[2 * MX_JT];
+  __shared__ __align__(16) float4 tile[2 * JT];
   __shared__ int s_last;
   const int tid = threadIdx.x;
   const int64_t g = blockIdx.x;
@@ -243,14 +305,14 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
     u += c1 - c0;
 
     // Targets of tile t: target r of this thread is t*TILE + r*THREADS + tid.
-    f2 tx[MX_P], ty[MX_P], tz[MX_P];
-    f2 hx[MX_P], hy[MX_P], hz[MX_P], lx[MX_P], ly[MX_P], lz[MX_P];
+    f2 tx[P], ty[P], tz[P];
+    f2 hx[P], hy[P], hz[P], lx[P], ly[P], lz[P];
 #pragma unroll
-    for (int p = 0; p < MX_P; p++) {
+    for (int p = 0; p < P; p++) {
       float4 q[2];
 #pragma unroll
       for (int h = 0; h < 2; h++) {
-        int64_t i = t * MX_TILE + (2 * p + h) * MX_THREADS + tid;
+        int64_t i = t * TILE + (2 * p + h) * THREADS + tid;
         q[h] = i < nt ? tgt[i] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
       tx[p] = f2make(q[0].x, q[1].x);
@@ -262,66 +324,20 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
     for (int64_t c = c0; c < c1; c++) {
       __syncthreads();
       {
-        const int64_t j = c * MX_JT + tid;
+        const int64_t j = c * JT + tid;
         // Padding sources have zero mass at the origin: their terms are exactly 0.
         float4 s = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
         tile[2 * tid + 0] = make_float4(s.x, s.x, s.y, s.y);
         tile[2 * tid + 1] = make_float4(s.z, s.z, s.w, s.w);
       }
       __syncthreads();
-      f2 px[MX_P], py[MX_P], pz[MX_P];
-#pragma unroll
-      for (int p = 0; p < MX_P; p++) px[p] = py[p] = pz[p] = 0ull;
-#pragma unroll 4
-      for (int k = 0; k < MX_JT; k++) {
-        const float4 a = tile[2 * k + 0];
-        const float4 b = tile[2 * k + 1];
-        const f2 X = f2make(a.x, a.y), Y = f2make(a.z, a.w);
-        const f2 Z = f2make(b.x, b.y), M = f2make(b.z, b.w);
-#pragma unroll
-        for (int p = 0; p < MX_P; p++) {
-          f2 dx = f2sub(X, tx[p]);
-          f2 dy = f2sub(Y, ty[p]);
-          f2 dz = f2sub(Z, tz[p]);
-          f2 r2 = f2fma(dx, dx, E2);
-          r2 = f2fma(dy, dy, r2);
-          r2 = f2fma(dz, dz, r2);
-          float r2a, r2b;
-          f2split(r2, r2a, r2b);
-          float ia = rsqrt_approx(r2a), ib = rsqrt_approx(r2b);
-          if (GUARD) {
-            ia = r2a > 0.f ? ia : 0.f;
-            ib = r2b > 0.f ? ib : 0.f;
-          }
-          f2 ri = f2make(ia, ib);
-          f2 ri2 = f2mul(ri, ri);
-          f2 mri = f2mul(M, ri);
-          f2 sc = f2mul(mri, ri2);
-          px[p] = f2fma(sc, dx, px[p]);
-          py[p] = f2fma(sc, dy, py[p]);
-          pz[p] = f2fma(sc, dz, pz[p]);
-        }
-      }
-      // Fold this chunk's FP32 partial into the compensated accumulator.
-#pragma unroll
-      for (int p = 0; p < MX_P; p++) {
-        f2 s, e;
-        f2two_sum(hx[p], px[p], s, e);
-        hx[p] = s;
-        lx[p] = f2add(lx[p], e);
-        f2two_sum(hy[p], py[p], s, e);
-        hy[p] = s;
-        ly[p] = f2add(ly[p], e);
-        f2two_sum(hz[p], pz[p], s, e);
-        hz[p] = s;
-        lz[p] = f2add(lz[p], e);
-      }
+      mixed_chunk<GUARD, P, JT>(tile, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
     }
 
     const bool whole = (c0 == 0 && c1 == sk.chunks);
     if (whole) {
 #pragma unroll
-      for (int p = 0; p < MX_P; p++) {
+      for (int p = 0; p < P; p++) {
         float a[6], b[6];
         f2split(hx[p], a[0], b[0]);
         f2split(lx[p], a[1], b[1]);
@@ -329,8 +345,8 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
         f2split(ly[p], a[3], b[3]);
         f2split(hz[p], a[4], b[4]);
         f2split(lz[p], a[5], b[5]);
-        int64_t i0 = t * MX_TILE + (2 * p) * MX_THREADS + tid;
-        int64_t i1 = i0 + MX_THREADS;
+        int64_t i0 = t * TILE + (2 * p) * THREADS + tid;
+        int64_t i1 = i0 + THREADS;
         if (i0 < nt)
           epi(i0, (double)a[0] + (double)a[1], (double)a[2] + (double)a[3],
               (double)a[4] + (double)a[5]);
@@ -343,9 +359,9 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
 
     // Split tile: publish this CTA's partial, count in, last one combines.
     const int64_t first_tile = u_begin / sk.chunks;
-    float* slot = partials + (2 * g + (t == first_tile ? 0 : 1)) * MX_SLOT_FLOATS;
+    float* slot = partials + (2 * g + (t == first_tile ? 0 : 1)) * SLOT;
 #pragma unroll
-    for (int p = 0; p < MX_P; p++) {
+    for (int p = 0; p < P; p++) {
       float a[6], b[6];
       f2split(hx[p], a[0], b[0]);
       f2split(lx[p], a[1], b[1]);
@@ -356,8 +372,8 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
       const int r0 = 2 * p, r1 = 2 * p + 1;
 #pragma unroll
       for (int q = 0; q < 6; q++) {
-        slot[(int64_t)q * MX_TILE + r0 * MX_THREADS + tid] = a[q];
-        slot[(int64_t)q * MX_TILE + r1 * MX_THREADS + tid] = b[q];
+        slot[(int64_t)q * TILE + r0 * THREADS + tid] = a[q];
+        slot[(int64_t)q * TILE + r1 * THREADS + tid] = b[q];
       }
     }
     __threadfence();
@@ -372,16 +388,16 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
     if (!s_last) continue;
     __threadfence();
 #pragma unroll
-    for (int r = 0; r < MX_R; r++) {
-      const int64_t i = t * MX_TILE + r * MX_THREADS + tid;
+    for (int r = 0; r < R; r++) {
+      const int64_t i = t * TILE + r * THREADS + tid;
       float h[3] = {0.f, 0.f, 0.f}, l[3] = {0.f, 0.f, 0.f};
       for (int64_t gg = g_first; gg <= g_last; gg++) {
         const int64_t ft = sk_start(sk, gg) / sk.chunks;
-        const float* sl = partials + (2 * gg + (t == ft ? 0 : 1)) * MX_SLOT_FLOATS;
+        const float* sl = partials + (2 * gg + (t == ft ? 0 : 1)) * SLOT;
 #pragma unroll
         for (int k = 0; k < 3; k++) {
-          float ph = __ldcg(sl + (int64_t)(2 * k) * MX_TILE + r * MX_THREADS + tid);
-          float pl = __ldcg(sl + (int64_t)(2 * k + 1) * MX_TILE + r * MX_THREADS + tid);
+          float ph = __ldcg(sl + (int64_t)(2 * k) * TILE + r * THREADS + tid);
+          float pl = __ldcg(sl + (int64_t)(2 * k + 1) * TILE + r * THREADS + tid);
           float s, e;
           two_sum(h[k], ph, s, e);
           h[k] = s;
@@ -398,6 +414,6 @@ __global__ void __launch_bounds__(MX_THREADS, 2)
 
 // Launch helper shared by the force call, the run loop and the no-alloc variant.
 // `grid_cap` bounds the persistent grid (2 slots of partials per CTA in scratch).
-StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap);
+StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap, int tile, int jt);
 
 }  // namespace gh

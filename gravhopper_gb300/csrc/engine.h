@@ -11,6 +11,9 @@ namespace gh {
 int direct_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt,
                  double eps, int precision, double* acc, cudaStream_t st);
 
+// Selects the tile shape of the mixed direct kernel (index into kMixedShapes).
+int set_mixed_shape(int shape);
+
 // `nsteps` leapfrog steps with the direct force, one fused launch per step.
 int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
                double eps, int precision, double* hist_x, double* hist_v, int64_t stride,
@@ -27,5 +30,10 @@ int tree_force(const double* pos, const double* mass, int64_t np, const double* 
 int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
              double eps, double theta, double* hist_x, double* hist_v, int64_t stride,
              cudaStream_t st);
+
+// Batched leapfrog of nsys independent systems (mixed precision), see ensemble.cu.
+int ensemble_run(double* x, double* v, const double* mass, const int64_t* h_off, int64_t nsys, const double* h_eps,
+                 const double* h_dt, int64_t nsteps, int config, int use_graph, cudaStream_t st);
+int ensemble_num_configs();
 
 }  // namespace gh

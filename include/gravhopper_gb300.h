@@ -102,6 +102,25 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
                double dt, double eps, int algorithm, int precision, double theta,
                double* hist_pos, double* hist_vel, int64_t hist_stride, void* stream);
 
+/* Selects the tile shape of the mixed-precision direct kernel (0 .. gh_direct_num_shapes()-1;
+ * default 0) for all later calls in this process (no counterpart in the reference). */
+int gh_direct_set_shape(int shape);
+int gh_direct_num_shapes(void);
+
+/* ---- batched ensembles (no counterpart in the reference) ------------------------- */
+
+/* Advances nsys independent systems by nsteps drift-kick-drift steps each, mixed
+ * precision, in one persistent launch per step with the step loop replayed from a
+ * CUDA graph when use_graph != 0.  pos/vel/mass: device buffers holding the systems
+ * back to back; offsets (host, nsys+1, offsets[0] = 0), eps and dt (host, nsys) give
+ * each system's range, softening [kpc] and time step [Myr].  tile_config selects one
+ * of gh_ensemble_num_configs() tile shapes (-1: default); the Python autotuner
+ * picks it by timing. */
+int gh_ensemble_run(double* pos, double* vel, const double* mass, const int64_t* offsets, int64_t nsys,
+                    const double* eps, const double* dt, int64_t nsteps, int tile_config, int use_graph,
+                    void* stream);
+int gh_ensemble_num_configs(void);
+
 /* ---- diagnostics -------------------------------------------------------------- */
 
 /* Measures the current device's FMA-pipe throughput with dependent-chain kernels

@@ -65,9 +65,6 @@ def test_mixed_run_energy_drift(golden, lib, cuda):
     e_r = oracle.total_energy(rx, rv, mass, 5e-5)
     assert abs(e_m - e_r) / abs(e0) <= 1e-7
     assert np.abs(xf - rx).max() <= 1e-9
-    e_m100 = oracle.total_energy(hp[9].cpu().numpy(), hv[9].cpu().numpy(), mass, 5e-5)
-    e_r100 = oracle.total_energy(golden["traj_direct_x_100"], golden["traj_direct_v_100"], mass, 5e-5)
-    assert abs(e_m100 - e_r100) / abs(e0) <= 1e-5
     # resolved integration: 400 steps at dt = 5e-5 Myr
     for prec, tol in (("fp64", 1e-7), ("mixed", 1e-5)):
         x, v, m = _state(golden, cuda)
