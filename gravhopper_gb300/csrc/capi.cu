@@ -155,6 +155,17 @@ int gh_ensemble_run(double* pos, double* vel, const double* mass, const int64_t*
 
 int gh_ensemble_num_configs(void) { return ensemble_num_configs(); }
 
+int gh_direct_vjp_dev(const double* pos, const double* mass, int64_t np, double eps, const double* cot,
+                      int precision, double* grad_pos, double* grad_mass, void* stream) {
+  clear_error();
+  return direct_vjp(pos, mass, np, eps, cot, precision, grad_pos, grad_mass, (cudaStream_t)stream);
+}
+
+int gh_potential_dev(const double* pos, const double* mass, int64_t np, double eps, double* phi, void* stream) {
+  clear_error();
+  return potential(pos, mass, np, eps, phi, (cudaStream_t)stream);
+}
+
 int gh_direct_set_shape(int shape) {
   clear_error();
   return set_mixed_shape(shape);

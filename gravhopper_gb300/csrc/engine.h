@@ -31,6 +31,14 @@ int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nstep
              double eps, double theta, double* hist_x, double* hist_v, int64_t stride,
              cudaStream_t st);
 
+// VJP of the direct-sum acceleration (adjoint.cu): cotangent lam (N,3) -> gradients
+// with respect to positions (N,3) and masses (N, may be null).
+int direct_vjp(const double* pos, const double* mass, int64_t n, double eps, const double* lam, int precision,
+               double* gpos, double* gmass, cudaStream_t st);
+
+// Per-particle softened potential phi_k = -sum_{j != k} m_j / sqrt(r^2 + eps^2) (G=1).
+int potential(const double* pos, const double* mass, int64_t n, double eps, double* phi, cudaStream_t st);
+
 // Batched leapfrog of nsys independent systems (mixed precision), see ensemble.cu.
 int ensemble_run(double* x, double* v, const double* mass, const int64_t* h_off, int64_t nsys, const double* h_eps,
                  const double* h_dt, int64_t nsteps, int config, int use_graph, cudaStream_t st);

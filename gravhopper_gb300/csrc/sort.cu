@@ -86,7 +86,8 @@ __global__ void __launch_bounds__(RS_THREADS)
   __shared__ uint32_t warp_off[NW][RS_BINS];
   __shared__ uint32_t cursor[RS_BINS];
   __shared__ uint32_t round_tot[RS_BINS];
-  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  static_assert(RS_THREADS == RS_BINS, "one digit bin per thread");
+  const int tid = threadIdx.x, warp = tid >> 5;
 #pragma unroll
   for (int k = 0; k < NW; k++) warp_cnt[k][tid] = 0;
   cursor[tid] = hist[(int64_t)tid * nb + blockIdx.x];

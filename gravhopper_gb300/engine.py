@@ -76,3 +76,41 @@ def run_dkd(pos, vel, mass, nsteps, dt, eps, algorithm="direct", precision="fp64
                float(eps), _capi.ALGORITHMS[algorithm], _capi.PRECISIONS[precision], float(theta),
                _capi.ptr(hp), _capi.ptr(hv), int(hist_stride), _capi.stream_handle(stream))
     return (hp, hv) if hist_stride > 0 else None
+
+
+def direct_vjp(pos, mass, eps, cot, precision="fp64", grad_pos=None, grad_mass=None, stream=None):
+    """Vector-Jacobian product of the direct-sum self-acceleration (code units).
+
+    Returns (grad_pos (N,3), grad_mass (N)) = (cot . da/dx, cot . da/dm).
+    """
+    _check(pos, "pos", 3)
+    _check(mass, "mass")
+    _check(cot, "cot", 3)
+    n = pos.shape[0]
+    if grad_pos is None:
+        grad_pos = torch.empty((n, 3), dtype=torch.float64, device=pos.device)
+    if grad_mass is None:
+        grad_mass = torch.empty(n, dtype=torch.float64, device=pos.device)
+    _capi.call("gh_direct_vjp_dev", _capi.ptr(pos), _capi.ptr(mass), n, float(eps), _capi.ptr(cot),
+               _capi.PRECISIONS[precision], _capi.ptr(grad_pos), _capi.ptr(grad_mass), _capi.stream_handle(stream))
+    return grad_pos, grad_mass
+
+
+def potential(pos, mass, eps, out=None, stream=None):
+    """Per-particle softened potential -sum_{j!=k} m_j / sqrt(r^2+eps^2) (G=1), FP64."""
+    _check(pos, "pos", 3)
+    _check(mass, "mass")
+    n = pos.shape[0]
+    if out is None:
+        out = torch.empty(n, dtype=torch.float64, device=pos.device)
+    _capi.call("gh_potential_dev", _capi.ptr(pos), _capi.ptr(mass), n, float(eps), _capi.ptr(out),
+               _capi.stream_handle(stream))
+    return out
+
+
+def energy(pos, vel, mass, eps):
+    """(kinetic, potential, total) energy in Msun (km/s)^2, on the device in FP64."""
+    from .units import G_KPC_KMS2_MSUN
+    ke = 0.5 * float(torch.sum(mass * torch.sum(vel * vel, dim=1)))
+    pe = 0.5 * G_KPC_KMS2_MSUN * float(torch.sum(mass * potential(pos, mass, eps)))
+    return ke, pe, ke + pe

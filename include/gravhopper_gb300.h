@@ -107,6 +107,19 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
 int gh_direct_set_shape(int shape);
 int gh_direct_num_shapes(void);
 
+/* ---- adjoint and diagnostics of the direct sum (no counterpart in the reference) ---- */
+
+/* Vector-Jacobian product of the direct-sum self-acceleration a(x, m) (code units):
+ * given the cotangent cot (np,3) of a, writes grad_pos (np,3) = sum_i cot_i . da_i/dx
+ * (the softened tidal tensor contracted with cot) and, when grad_mass is non-NULL,
+ * grad_mass (np) = sum_i cot_i . da_i/dm.  precision GH_PREC_FP64 or GH_PREC_MIXED. */
+int gh_direct_vjp_dev(const double* pos, const double* mass, int64_t np, double eps, const double* cot,
+                      int precision, double* grad_pos, double* grad_mass, void* stream);
+
+/* Per-particle softened potential phi (np) = -sum_{j != k} m_j / sqrt(r^2 + eps^2), code
+ * units (G=1), FP64.  Potential energy = 0.5 * G * sum_k m_k phi_k. */
+int gh_potential_dev(const double* pos, const double* mass, int64_t np, double eps, double* phi, void* stream);
+
 /* ---- batched ensembles (no counterpart in the reference) ------------------------- */
 
 /* Advances nsys independent systems by nsteps drift-kick-drift steps each, mixed
