@@ -75,6 +75,7 @@ SIGNATURES = {
     "gh_ensemble_run": (_int, [_vp, _vp, _vp, _vp, _i64, _vp, _vp, _i64, _int, _int, _vp]),
     "gh_ensemble_num_configs": (_int, []),
     "gh_direct_set_shape": (_int, [_int]),
+    "gh_direct_mixed_noalloc": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_direct_vjp_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _int, _vp, _vp, _vp]),
     "gh_potential_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_direct_num_shapes": (_int, []),

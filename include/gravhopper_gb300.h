@@ -102,6 +102,21 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
                double dt, double eps, int algorithm, int precision, double theta,
                double* hist_pos, double* hist_vel, int64_t hist_stride, void* stream);
 
+/* Mixed-precision direct-sum self-force (as gh_direct_dev with force_pos == NULL and
+ * GH_PREC_MIXED) that allocates no device memory.  No counterpart in the reference:
+ * it is for callers that cannot let a library allocate, such as an application
+ * that owns all device memory through its own pool, or a stepping loop that must not
+ * call cudaMalloc/cudaFree because those can synchronise the device.  The caller
+ * passes device inputs pos (np,3), mass (np) and the output acc (np,3); all scratch
+ * lives in one fixed ~16 MiB array in this library's device memory, held by every GPU
+ * that loads the library until the process exits.  np above 65536 is rejected with
+ * GH_ERR_ARG.  The first call on a device looks up that array's device address (make
+ * this first call before any stream capture).  Every call shares the array: calls
+ * that overlap on the GPU (different streams, or threads) race and must not be
+ * issued. */
+int gh_direct_mixed_noalloc(const double* pos, const double* mass, int64_t np, double eps, double* acc,
+                            void* stream);
+
 /* Selects the tile shape of the mixed-precision direct kernel (0 .. gh_direct_num_shapes()-1;
  * default 0) for all later calls in this process (no counterpart in the reference). */
 int gh_direct_set_shape(int shape);
