@@ -303,6 +303,133 @@ def measure_secondary(ic, dev, fp64_peak, mixed_gpair):
     out["mixed_rel_err_rms"] = float(torch.sqrt(torch.mean(err * err)))
     out["mixed_rel_err_max"] = float(err.max())
     out["mixed_err_sample"] = f"{idx.numel()} targets of N={n} vs FP64 form"
+    del x, m, a_mixed, a64
+    out["energy_drift_10_steps"] = measure_energy_drift(dev)
+    out["tree"] = measure_tree(dev)
+    out["ensemble"] = measure_ensemble(dev)
+    out["adjoint"] = measure_adjoint(dev)
+    return out
+
+
+def _timed(fn):
+    import torch
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    fn()
+    torch.cuda.synchronize()
+    return time.perf_counter() - t0
+
+
+def measure_energy_drift(dev, n=262144, steps=10):
+    """Config-1 energy drift |E(10) - E(0)| / |E(0)| for both forms (FP64 energies)."""
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    ic = ics.plummer(n, seed=5)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    out = {"n": n, "steps": steps}
+    e0 = None
+    for prec in ("fp64", "mixed"):
+        x = torch.from_numpy(ic["pos"]).to(dev)
+        v = torch.from_numpy(ic["vel"]).to(dev)
+        if e0 is None:
+            e0 = engine.energy(x, v, m, 5e-5)[2]
+        engine.run_dkd(x, v, m, steps, 0.005, 5e-5, algorithm="direct", precision=prec)
+        out[prec] = abs(engine.energy(x, v, m, 5e-5)[2] - e0) / abs(e0)
+    return out
+
+
+def measure_tree(dev, n=1 << 20, steps=2):
+    """Config 2: Hernquist + exponential disk, particle-steps/s of DKD steps with the tree."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import _capi, engine, ics
+    from oracle import oracle
+    ic = ics.hernquist_disk(n, seed=1)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    out = {"n": n, "workload": "Hernquist (70%) + exponential disk (30%), 1e11 Msun, eps=0.1 kpc, dt=0.5 Myr"}
+    for theta in (0.7, 0.5):
+        x = torch.from_numpy(ic["pos"]).to(dev)
+        v = torch.from_numpy(ic["vel"]).to(dev)
+        engine.run_dkd(x, v, m, 1, 0.5, 0.1, algorithm="tree", theta=theta)
+        _capi.kernel_timing_collect()
+        _capi.kernel_timing(True)
+        t = _timed(lambda: engine.run_dkd(x, v, m, steps, 0.5, 0.1, algorithm="tree", theta=theta))
+        _capi.kernel_timing(False)
+        walk_ms, walks = _capi.kernel_timing_collect()
+        key = f"theta_{theta}"
+        out[key] = {"particle_steps_per_s": n * steps / t, "ms_per_step": t / steps * 1e3,
+                    "walk_ms_per_step": walk_ms / max(walks, 1), "build_ms_per_step": t / steps * 1e3 -
+                    walk_ms / max(walks, 1)}
+    # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
+    # full serial build plus the walk of 2048 targets, scaled to all N targets.
+    rng = np.random.default_rng(0)
+    idx = rng.choice(n, size=2048, replace=False)
+    for theta in (0.7, 0.5):
+        t0 = time.perf_counter()
+        oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx[:1]], 0.1, theta, nthreads=1)
+        t_build = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx], 0.1, theta,
+                                   nthreads=oracle.default_threads())
+        t_all = time.perf_counter() - t0
+        walk = max(t_all - t_build, 0.0) * n / idx.size
+        out[f"theta_{theta}"]["cpu_reference_s_per_step"] = t_build + walk
+        out[f"theta_{theta}"]["cpu_reference_cores"] = oracle.default_threads()
+    return out
+
+
+def measure_ensemble(dev, steps=50, loop_steps=10):
+    """Config 3: 512 Plummer spheres, N log-uniform in [256, 8192], one persistent launch
+    per step replayed from a CUDA graph, against integrating the systems one by one."""
+    from gravhopper_gb300 import ics
+    from gravhopper_gb300.ensemble import Ensemble, autotune, run_one_by_one
+    systems = ics.plummer_ensemble(512, seed=0)
+    e = Ensemble(systems, device=dev)
+    best, times = autotune(e, steps=2, use_cache=False)
+    e.run(2)
+    t = _timed(lambda: e.run(steps, use_graph=True))
+    f = Ensemble(systems, device=dev)
+    run_one_by_one(f, 1)
+    tl = _timed(lambda: run_one_by_one(f, loop_steps))
+    pairs = e.pairs_per_step
+    return {"systems": 512, "particles": int(e.offsets[-1]), "pairs_per_step": pairs, "tile_config": best,
+            "ms_per_step": t / steps * 1e3, "gpair_s": pairs / (t / steps) / 1e9,
+            "one_by_one_ms_per_step": tl / loop_steps * 1e3, "speedup_vs_one_by_one": (tl / loop_steps) / (t / steps)}
+
+
+def measure_adjoint(dev, n=16384, steps=200):
+    """Config 4: gradients of a 200-step mixed rollout (checkpoints every 20 steps)
+    with respect to x0, v0 and m; backward time over forward time."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    from gravhopper_gb300.adjoint import rollout
+    ic = ics.plummer(n, seed=0)
+    rng = np.random.default_rng(1)
+    x0 = torch.from_numpy(ic["pos"]).to(dev)
+    v0 = torch.from_numpy(ic["vel"]).to(dev)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
+    vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()
+    engine.run_dkd(xt, vt, m, steps, 0.005, 5e-5, precision="mixed")
+    out = {"n": n, "steps": steps}
+    for k in (20, 1):
+        for rep in range(2):  # first repetition warms up
+            xa, va, ma = (t.clone().requires_grad_(True) for t in (x0, v0, m))
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            xT, _ = rollout(xa, va, ma, steps, 0.005, 5e-5, checkpoint_every=k, precision="mixed")
+            loss = ((xT - xt) ** 2).mean()
+            torch.cuda.synchronize()
+            t1 = time.perf_counter()
+            loss.backward()
+            torch.cuda.synchronize()
+            t2 = time.perf_counter()
+        out[f"checkpoint_{k}"] = {"forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
+                                  "backward_over_forward": (t2 - t1) / (t1 - t0)}
     return out
 
 
