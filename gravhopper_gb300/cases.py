@@ -1,0 +1,63 @@
+"""Run one engine workload a few times and print its timing (for profiling).
+
+    python -m gravhopper_gb300.cases direct   --n 131072 --reps 2   # mixed direct force
+    python -m gravhopper_gb300.cases direct64 --n 65536  --reps 1   # FP64 direct force
+    python -m gravhopper_gb300.cases tree     --n 65536  --theta 0.7
+    python -m gravhopper_gb300.cases ensemble --systems 64
+    python -m gravhopper_gb300.cases vjp      --n 16384
+
+Each case builds seeded inputs (Plummer spheres; Hernquist plus disk for the tree),
+runs one warm-up call and ``--reps`` timed calls on cuda:0, and prints one line of
+milliseconds per call.
+"""
+from __future__ import annotations
+
+import argparse
+import time
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser()
+    ap.add_argument("case", choices=["direct", "direct64", "tree", "ensemble", "vjp"])
+    ap.add_argument("--n", type=int, default=131072)
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--theta", type=float, default=0.7)
+    ap.add_argument("--systems", type=int, default=64)
+    a = ap.parse_args(argv)
+
+    import torch
+
+    from . import _capi, engine, ics
+    dev = torch.device("cuda", 0)
+    _capi.load()
+    if a.case in ("direct", "direct64", "vjp"):
+        ic = ics.plummer(a.n, seed=0)
+    elif a.case == "tree":
+        ic = ics.hernquist_disk(a.n, seed=1)
+    if a.case == "ensemble":
+        from .ensemble import Ensemble
+        e = Ensemble(ics.plummer_ensemble(a.systems, seed=0), device=dev)
+        call = lambda: e.run(1, use_graph=False)  # noqa: E731
+    else:
+        x = torch.from_numpy(ic["pos"]).to(dev)
+        m = torch.from_numpy(ic["mass"]).to(dev)
+        if a.case == "direct":
+            call = lambda: engine.direct_force(x, m, 5e-5, precision="mixed")  # noqa: E731
+        elif a.case == "direct64":
+            call = lambda: engine.direct_force(x, m, 5e-5, precision="fp64")  # noqa: E731
+        elif a.case == "tree":
+            call = lambda: engine.tree_force(x, m, 0.1, a.theta)  # noqa: E731
+        else:
+            lam = torch.ones_like(x)
+            call = lambda: engine.direct_vjp(x, m, 5e-5, lam, precision="mixed")  # noqa: E731
+    call()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(a.reps):
+        call()
+    torch.cuda.synchronize()
+    print(f"{a.case} n={a.n} reps={a.reps}: {(time.perf_counter() - t0) / max(a.reps, 1) * 1e3:.3f} ms per call")
+
+
+if __name__ == "__main__":
+    main()
