@@ -67,7 +67,7 @@ SIGNATURES = {
     "gh_direct_host": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _int, _vp]),
     "gh_tree_force": (_int, [_vp, _vp, _i64, _dbl, _dbl, _vp]),
     "gh_tree_force_position": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _vp]),
-    "gh_tree_dev": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _vp, _vp]),
+    "gh_tree_dev": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _int, _vp, _vp]),
     "gh_direct_dev": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _int, _vp, _vp]),
     "gh_run_dkd": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _int, _dbl, _vp, _vp, _i64,
                           _vp]),
@@ -78,6 +78,7 @@ SIGNATURES = {
     "gh_direct_mixed_noalloc": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_direct_vjp_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _int, _vp, _vp, _vp]),
     "gh_potential_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
+    "gh_dkd_backward_dev": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _vp, _vp, _vp, _vp]),
     "gh_direct_num_shapes": (_int, []),
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),

@@ -3,8 +3,8 @@
 ``rollout(x0, v0, m, nsteps, dt, eps)`` is a ``torch.autograd.Function``: the forward
 pass runs the drift-kick-drift leapfrog on the GPU (gravhopper/gravhopper.py:405-416
 arithmetic), keeping the state every ``checkpoint_every`` steps; the backward pass
-walks the segments in reverse, recomputes each segment's states from its checkpoint,
-and back-propagates step by step:
+walks the segments in reverse and hands each to ``gh_dkd_backward_dev``, which
+recomputes the segment's states from its checkpoint and back-propagates step by step:
 
     forward:  xh = x + c v,  a = A F(xh, m),  v' = v + dt a,  x' = xh + c v'
     backward: w = v'bar + c x'bar,  lam = A dt w,  (gx, gm) = VJP of F at xh with lam,
@@ -18,8 +18,7 @@ from __future__ import annotations
 
 import torch
 
-from . import engine
-from .units import ACCEL_UNIT, KMS_MYR_TO_KPC
+from . import _capi, engine
 
 
 class _Rollout(torch.autograd.Function):
@@ -45,31 +44,14 @@ class _Rollout(torch.autograd.Function):
     def backward(ctx, gx, gv):
         (m,) = ctx.saved_tensors
         dt, eps, precision = ctx.params
-        c = 0.5 * dt * KMS_MYR_TO_KPC
         n = m.shape[0]
         xb = gx.contiguous().clone() if gx is not None else torch.zeros((n, 3), dtype=torch.float64, device=m.device)
         vb = gv.contiguous().clone() if gv is not None else torch.zeros_like(xb)
         mb = torch.zeros_like(m)
-        gpos = torch.empty_like(xb)
-        gmass = torch.empty_like(m)
         for xs, vs, seg in reversed(ctx.ckpts):
-            states = [(xs, vs)]
-            if seg > 1:
-                x = xs.clone()
-                v = vs.clone()
-                hp, hv = engine.run_dkd(x, v, m, seg - 1, dt, eps, algorithm="direct", precision=precision,
-                                        hist_stride=1)
-                states += [(hp[j], hv[j]) for j in range(seg - 1)]
-            for xj, vj in reversed(states):
-                xh = xj + ((0.5 * vj) * dt) * KMS_MYR_TO_KPC
-                w = vb + c * xb
-                lam = (ACCEL_UNIT * dt) * w
-                engine.direct_vjp(xh.contiguous(), m, eps, lam.contiguous(), precision=precision,
-                                  grad_pos=gpos, grad_mass=gmass)
-                xhb = xb + gpos
-                mb += gmass
-                vb = w + c * xhb
-                xb = xhb
+            _capi.call("gh_dkd_backward_dev", _capi.ptr(xs), _capi.ptr(vs), _capi.ptr(m), n, int(seg), float(dt),
+                       float(eps), _capi.PRECISIONS[precision], _capi.ptr(xb), _capi.ptr(vb), _capi.ptr(mb),
+                       _capi.stream_handle())
         ctx.ckpts = None
         return xb, vb, mb, None, None, None, None, None
 

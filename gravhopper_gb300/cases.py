@@ -2,7 +2,7 @@
 
     python -m gravhopper_gb300.cases direct   --n 131072 --reps 2   # mixed direct force
     python -m gravhopper_gb300.cases direct64 --n 65536  --reps 1   # FP64 direct force
-    python -m gravhopper_gb300.cases tree     --n 65536  --theta 0.7
+    python -m gravhopper_gb300.cases tree     --n 65536  --theta 0.7 --precision fp64
     python -m gravhopper_gb300.cases ensemble --systems 64
     python -m gravhopper_gb300.cases vjp      --n 16384
 
@@ -23,6 +23,7 @@ def main(argv=None):
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--theta", type=float, default=0.7)
     ap.add_argument("--systems", type=int, default=64)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="tree and vjp cases")
     a = ap.parse_args(argv)
 
     import torch
@@ -46,10 +47,10 @@ def main(argv=None):
         elif a.case == "direct64":
             call = lambda: engine.direct_force(x, m, 5e-5, precision="fp64")  # noqa: E731
         elif a.case == "tree":
-            call = lambda: engine.tree_force(x, m, 0.1, a.theta)  # noqa: E731
+            call = lambda: engine.tree_force(x, m, 0.1, a.theta, precision=a.precision)  # noqa: E731
         else:
             lam = torch.ones_like(x)
-            call = lambda: engine.direct_vjp(x, m, 5e-5, lam, precision="mixed")  # noqa: E731
+            call = lambda: engine.direct_vjp(x, m, 5e-5, lam, precision=a.precision)  # noqa: E731
     call()
     torch.cuda.synchronize()
     t0 = time.perf_counter()

@@ -86,62 +86,157 @@ __global__ void __launch_bounds__(AJ_THREADS)
 }
 
 // ---------------------------------------------------------------------------
-// Mixed VJP: FP32 pairs, 8 floats of partials per (split, target): hi/lo of gx..gm.
+// Mixed VJP: FP32 pair arithmetic on packed f32x2 lanes (two targets per thread
+// register pair, VJ_P packs per thread), sources duplicated per lane pair in shared
+// memory, per-chunk partials folded into two-sum (hi, lo) accumulators; 8 floats of
+// partials per (split, target): hi/lo of gx, gy, gz, gm.  Per pair: 30 FP32 lane-ops
+// (3 sub, 3 fma for s, 4 for q and -3q/s, 6 for u, 3 for d.u, 1, 6 for g, 4 for gm)
+// and one MUFU rsqrt.
 // ---------------------------------------------------------------------------
-constexpr int AJ_CHUNK = AJ_THREADS;
+constexpr int VJ_THREADS = 128;
+constexpr int VJ_P = 2;
+constexpr int VJ_TILE = VJ_THREADS * 2 * VJ_P;
+constexpr int VJ_JT = VJ_THREADS;
 
-__global__ void __launch_bounds__(AJ_THREADS)
-    vjp_mixed_kernel(const float4* __restrict__ src, const float4* __restrict__ lsrc, int64_t n, float eps2,
-                     int64_t jlen, float* __restrict__ part) {
-  __shared__ float4 sp[AJ_CHUNK], sl[AJ_CHUNK];
-  const int64_t k = (int64_t)blockIdx.x * AJ_THREADS + threadIdx.x;
-  const int64_t split = blockIdx.y;
-  const int64_t j0 = split * jlen, j1 = (j0 + jlen) < n ? j0 + jlen : n;
-  const bool valid = k < n;
-  const float4 T = valid ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float4 TL = valid ? lsrc[k] : make_float4(0.f, 0.f, 0.f, 0.f);
-  float h[4] = {0.f, 0.f, 0.f, 0.f}, l[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int64_t c = j0; c < j1; c += AJ_CHUNK) {
-    __syncthreads();
-    const int64_t j = c + threadIdx.x;
-    // padding and the target itself contribute nothing: zero mass and zero lambda
-    sp[threadIdx.x] = j < j1 ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-    sl[threadIdx.x] = j < j1 ? lsrc[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-    __syncthreads();
-    float gx = 0.f, gy = 0.f, gz = 0.f, gm = 0.f;
-#pragma unroll 4
-    for (int t = 0; t < AJ_CHUNK; t++) {
-      const float4 P = sp[t], L = sl[t];
-      const float dx = P.x - T.x, dy = P.y - T.y, dz = P.z - T.z;
-      const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2)));
-      float r = rsqrt_approx(s);
-      r = (c + t == k || !(s > 0.f)) ? 0.f : r;
-      const float r2 = r * r;
-      const float q = r2 * r;
-      const float p = 3.f * q * r2;
-      const float ux = fmaf(T.w, L.x, -P.w * TL.x), uy = fmaf(T.w, L.y, -P.w * TL.y),
-                  uz = fmaf(T.w, L.z, -P.w * TL.z);
-      const float pd = p * fmaf(dx, ux, fmaf(dy, uy, dz * uz));
-      gx = fmaf(q, ux, fmaf(-pd, dx, gx));
-      gy = fmaf(q, uy, fmaf(-pd, dy, gy));
-      gz = fmaf(q, uz, fmaf(-pd, dz, gz));
-      gm = fmaf(-q, fmaf(L.x, dx, fmaf(L.y, dy, L.z * dz)), gm);
-    }
-    const float pv[4] = {gx, gy, gz, gm};
+template <bool SELFCHK>
+__device__ __forceinline__ void vjp_chunk(const float4* __restrict__ tile, int64_t jbase, const int64_t* ka,
+                                          const f2* tx, const f2* ty, const f2* tz, const f2* tm, const f2* tlx,
+                                          const f2* tly, const f2* tlz, f2 E2, f2* gx, f2* gy, f2* gz, f2* gm) {
+  const f2 M3 = f2make(-3.f, -3.f);
+#pragma unroll 2
+  for (int k = 0; k < VJ_JT; k++) {
+    const float4 A = tile[4 * k], B = tile[4 * k + 1], C = tile[4 * k + 2], D = tile[4 * k + 3];
+    const f2 X = f2make(A.x, A.y), Y = f2make(A.z, A.w), Z = f2make(B.x, B.y), NM = f2make(B.z, B.w);
+    const f2 LX = f2make(C.x, C.y), LY = f2make(C.z, C.w), LZ = f2make(D.x, D.y);
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      float s, e;
-      two_sum(h[q], pv[q], s, e);
-      h[q] = s;
-      l[q] = __fadd_rn(l[q], e);
+    for (int p = 0; p < VJ_P; p++) {
+      const f2 dx = f2sub(X, tx[p]), dy = f2sub(Y, ty[p]), dz = f2sub(Z, tz[p]);
+      f2 s = f2fma(dx, dx, E2);
+      s = f2fma(dy, dy, s);
+      s = f2fma(dz, dz, s);
+      float sa, sb;
+      f2split(s, sa, sb);
+      float ra = rsqrt_approx(sa), rb = rsqrt_approx(sb);
+      if (SELFCHK) {
+        ra = (jbase + k == ka[2 * p]) ? 0.f : ra;
+        rb = (jbase + k == ka[2 * p + 1]) ? 0.f : rb;
+      }
+      const f2 r = f2make(ra, rb);
+      const f2 r2 = f2mul(r, r);
+      const f2 q = f2mul(r2, r);
+      const f2 np = f2mul(f2mul(q, M3), r2);
+      const f2 ux = f2fma(NM, tlx[p], f2mul(tm[p], LX));
+      const f2 uy = f2fma(NM, tly[p], f2mul(tm[p], LY));
+      const f2 uz = f2fma(NM, tlz[p], f2mul(tm[p], LZ));
+      f2 du = f2mul(dx, ux);
+      du = f2fma(dy, uy, du);
+      du = f2fma(dz, uz, du);
+      const f2 npd = f2mul(np, du);
+      gx[p] = f2fma(npd, dx, f2fma(q, ux, gx[p]));
+      gy[p] = f2fma(npd, dy, f2fma(q, uy, gy[p]));
+      gz[p] = f2fma(npd, dz, f2fma(q, uz, gz[p]));
+      f2 ld = f2mul(dx, LX);
+      ld = f2fma(dy, LY, ld);
+      ld = f2fma(dz, LZ, ld);
+      gm[p] = f2fma(q, ld, gm[p]);
     }
   }
-  if (valid) {
-    float* o = part + (split * n + k) * 8;
+}
+
+__global__ void __launch_bounds__(VJ_THREADS, 4)
+    vjp_mixed_kernel(const float4* __restrict__ src, const float4* __restrict__ lsrc, int64_t n, float eps2,
+                     int64_t jlen, float* __restrict__ part) {
+  __shared__ __align__(16) float4 tile[4 * VJ_JT];
+  const int tid = threadIdx.x;
+  const int64_t tbase = (int64_t)blockIdx.x * VJ_TILE;
+  const int64_t split = blockIdx.y;
+  const int64_t j0 = split * jlen, j1 = (j0 + jlen) < n ? j0 + jlen : n;
+  f2 tx[VJ_P], ty[VJ_P], tz[VJ_P], tm[VJ_P], tlx[VJ_P], tly[VJ_P], tlz[VJ_P];
+  f2 hx[VJ_P], hy[VJ_P], hz[VJ_P], hm[VJ_P], lx[VJ_P], ly[VJ_P], lz[VJ_P], lm[VJ_P];
+  int64_t ka[2 * VJ_P];
 #pragma unroll
-    for (int q = 0; q < 4; q++) {
-      o[2 * q] = h[q];
-      o[2 * q + 1] = l[q];
+  for (int p = 0; p < VJ_P; p++) {
+    float4 P0[2], L0[2];
+#pragma unroll
+    for (int h = 0; h < 2; h++) {
+      const int64_t k = tbase + (2 * p + h) * VJ_THREADS + tid;
+      ka[2 * p + h] = k;
+      P0[h] = k < n ? src[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      L0[h] = k < n ? lsrc[k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    tx[p] = f2make(P0[0].x, P0[1].x);
+    ty[p] = f2make(P0[0].y, P0[1].y);
+    tz[p] = f2make(P0[0].z, P0[1].z);
+    tm[p] = f2make(P0[0].w, P0[1].w);
+    tlx[p] = f2make(L0[0].x, L0[1].x);
+    tly[p] = f2make(L0[0].y, L0[1].y);
+    tlz[p] = f2make(L0[0].z, L0[1].z);
+    hx[p] = hy[p] = hz[p] = hm[p] = lx[p] = ly[p] = lz[p] = lm[p] = 0ull;
+  }
+  const f2 E2 = f2make(eps2, eps2);
+  for (int64_t c = j0; c < j1; c += VJ_JT) {
+    __syncthreads();
+    {
+      const int64_t j = c + tid;
+      const float4 P = j < j1 ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float4 L = j < j1 ? lsrc[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      tile[4 * tid + 0] = make_float4(P.x, P.x, P.y, P.y);
+      tile[4 * tid + 1] = make_float4(P.z, P.z, -P.w, -P.w);
+      tile[4 * tid + 2] = make_float4(L.x, L.x, L.y, L.y);
+      tile[4 * tid + 3] = make_float4(L.z, L.z, 0.f, 0.f);
+    }
+    __syncthreads();
+    f2 gx[VJ_P], gy[VJ_P], gz[VJ_P], gm[VJ_P];
+#pragma unroll
+    for (int p = 0; p < VJ_P; p++) gx[p] = gy[p] = gz[p] = gm[p] = 0ull;
+    // only a chunk that overlaps this tile's targets can pair a target with itself
+    if (c < tbase + VJ_TILE && c + VJ_JT > tbase)
+      vjp_chunk<true>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+    else
+      vjp_chunk<false>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+#pragma unroll
+    for (int p = 0; p < VJ_P; p++) {
+      f2 sm, e;
+      f2two_sum(hx[p], gx[p], sm, e);
+      hx[p] = sm;
+      lx[p] = f2add(lx[p], e);
+      f2two_sum(hy[p], gy[p], sm, e);
+      hy[p] = sm;
+      ly[p] = f2add(ly[p], e);
+      f2two_sum(hz[p], gz[p], sm, e);
+      hz[p] = sm;
+      lz[p] = f2add(lz[p], e);
+      f2two_sum(hm[p], gm[p], sm, e);
+      hm[p] = sm;
+      lm[p] = f2add(lm[p], e);
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < VJ_P; p++) {
+    float a[8], b[8];
+    f2split(hx[p], a[0], b[0]);
+    f2split(lx[p], a[1], b[1]);
+    f2split(hy[p], a[2], b[2]);
+    f2split(ly[p], a[3], b[3]);
+    f2split(hz[p], a[4], b[4]);
+    f2split(lz[p], a[5], b[5]);
+    f2split(hm[p], a[6], b[6]);
+    f2split(lm[p], a[7], b[7]);
+    // dL/dm_k = -sum q (lambda_j . d): the mass terms were accumulated with + sign
+    a[6] = -a[6];
+    a[7] = -a[7];
+    b[6] = -b[6];
+    b[7] = -b[7];
+    const int64_t k0 = ka[2 * p], k1 = ka[2 * p + 1];
+    if (k0 < n) {
+      float* o = part + (split * n + k0) * 8;
+#pragma unroll
+      for (int q = 0; q < 8; q++) o[q] = a[q];
+    }
+    if (k1 < n) {
+      float* o = part + (split * n + k1) * 8;
+#pragma unroll
+      for (int q = 0; q < 8; q++) o[q] = b[q];
     }
   }
 }
@@ -300,7 +395,6 @@ int direct_vjp(const double* pos, const double* mass, int64_t n, double eps, con
     GH_LAUNCH_CHECK();
     return GH_OK;
   }
-  GH_TRY(ensure(ws.part, (size_t)splits * n * 8 * sizeof(float)));
   GH_TRY(ensure(ws.src, (size_t)n * sizeof(float4)));
   GH_TRY(ensure(ws.lsrc, (size_t)n * sizeof(float4)));
   GH_TRY(ensure(ws.origin, 4 * sizeof(double)));
@@ -309,13 +403,105 @@ int direct_vjp(const double* pos, const double* mass, int64_t n, double eps, con
   vjp_prepare_mixed_kernel<<<rb, 256, 0, st>>>(pos, mass, lam, n, (const double*)ws.origin.ptr, (float4*)ws.src.ptr,
                                                (float4*)ws.lsrc.ptr);
   GH_LAUNCH_CHECK();
+  // Mixed kernel: tiles of VJ_TILE targets, splits of whole VJ_JT-source chunks,
+  // about four resident CTAs per SM, filled twice over.
+  const int64_t mtiles = (n + VJ_TILE - 1) / VJ_TILE;
+  const int64_t chunks = (n + VJ_JT - 1) / VJ_JT;
+  int64_t msplits = (8LL * di.num_sms + mtiles - 1) / mtiles;
+  if (msplits > chunks) msplits = chunks;
+  if (msplits < 1) msplits = 1;
+  const int64_t mjlen = ((chunks + msplits - 1) / msplits) * VJ_JT;
+  msplits = (n + mjlen - 1) / mjlen;
+  GH_TRY(ensure(ws.part, (size_t)msplits * n * 8 * sizeof(float)));
   prof_begin(st);
-  vjp_mixed_kernel<<<grid, AJ_THREADS, 0, st>>>((const float4*)ws.src.ptr, (const float4*)ws.lsrc.ptr, n,
-                                                (float)(eps * eps), jlen, (float*)ws.part.ptr);
+  vjp_mixed_kernel<<<dim3((unsigned)mtiles, (unsigned)msplits), VJ_THREADS, 0, st>>>(
+      (const float4*)ws.src.ptr, (const float4*)ws.lsrc.ptr, n, (float)(eps * eps), mjlen, (float*)ws.part.ptr);
   prof_end(st);
   GH_LAUNCH_CHECK();
-  vjp_reduce_mixed_kernel<<<rb, 256, 0, st>>>((const float*)ws.part.ptr, (int)splits, n, gpos, gmass);
+  vjp_reduce_mixed_kernel<<<rb, 256, 0, st>>>((const float*)ws.part.ptr, (int)msplits, n, gpos, gmass);
   GH_LAUNCH_CHECK();
+  return GH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Backward pass of drift-kick-drift steps.  Forward step (gravhopper.py:405-416):
+//   xh = x + c v,  v' = v + dt A F(xh),  x' = xh + c v'      (c = 0.5 dt F_kpc)
+// Reverse, given (xbar, vbar) of (x', v'):
+//   w = vbar + c xbar;  lam = A dt w;  (gx, gm) = VJP of F at xh with lam;
+//   xhbar = xbar + gx;  xbar <- xhbar;  vbar <- w + c xhbar;  mbar += gm
+// ---------------------------------------------------------------------------
+__global__ void adj_pre_kernel(const double* __restrict__ x, const double* __restrict__ v, int64_t n, double dt,
+                               const double* __restrict__ xbar, const double* __restrict__ vbar,
+                               double* __restrict__ xh, double* __restrict__ w, double* __restrict__ lam) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * n) return;
+  const double c = 0.5 * dt * GH_KMS_MYR_TO_KPC;
+  xh[i] = drift_half(x[i], v[i], dt);
+  const double wi = vbar[i] + c * xbar[i];
+  w[i] = wi;
+  lam[i] = (GH_ACCEL_UNIT * dt) * wi;
+}
+
+__global__ void adj_post_kernel(int64_t n, double dt, const double* __restrict__ w, const double* __restrict__ gpos,
+                                const double* __restrict__ gmass, double* __restrict__ xbar,
+                                double* __restrict__ vbar, double* __restrict__ mbar) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < 3 * n) {
+    const double c = 0.5 * dt * GH_KMS_MYR_TO_KPC;
+    const double xhb = xbar[i] + gpos[i];
+    xbar[i] = xhb;
+    vbar[i] = w[i] + c * xhb;
+  }
+  if (i < n && mbar) mbar[i] += gmass[i];
+}
+
+struct BwdWS {
+  Buffer states_x, states_v, work_x, work_v, xh, w, lam, gpos, gmass;
+};
+static BwdWS g_bwd[64];
+static std::mutex g_bwd_mu;
+
+int dkd_backward(const double* x0, const double* v0, const double* mass, int64_t n, int64_t nsteps, double dt,
+                 double eps, int precision, double* xbar, double* vbar, double* mbar, cudaStream_t st) {
+  if (n < 0 || nsteps < 0) return set_error(GH_ERR_ARG, "negative n or nsteps");
+  if (n == 0 || nsteps == 0) return GH_OK;
+  if (!x0 || !v0 || !mass || !xbar || !vbar) return set_error(GH_ERR_ARG, "null buffer");
+  std::lock_guard<std::mutex> lk(g_bwd_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  BwdWS& ws = g_bwd[di.device];
+  const size_t vec = (size_t)n * 3 * sizeof(double);
+  GH_TRY(ensure(ws.states_x, vec * nsteps));
+  GH_TRY(ensure(ws.states_v, vec * nsteps));
+  GH_TRY(ensure(ws.work_x, vec));
+  GH_TRY(ensure(ws.work_v, vec));
+  GH_TRY(ensure(ws.xh, vec));
+  GH_TRY(ensure(ws.w, vec));
+  GH_TRY(ensure(ws.lam, vec));
+  GH_TRY(ensure(ws.gpos, vec));
+  GH_TRY(ensure(ws.gmass, (size_t)n * sizeof(double)));
+  double* sx = (double*)ws.states_x.ptr;
+  double* sv = (double*)ws.states_v.ptr;
+  // states[j] = state at the start of step j, j = 0 .. nsteps-1, recomputed from x0, v0
+  GH_CUDA_TRY(cudaMemcpyAsync(sx, x0, vec, cudaMemcpyDeviceToDevice, st));
+  GH_CUDA_TRY(cudaMemcpyAsync(sv, v0, vec, cudaMemcpyDeviceToDevice, st));
+  if (nsteps > 1) {
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.work_x.ptr, x0, vec, cudaMemcpyDeviceToDevice, st));
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.work_v.ptr, v0, vec, cudaMemcpyDeviceToDevice, st));
+    GH_TRY(direct_run((double*)ws.work_x.ptr, (double*)ws.work_v.ptr, mass, n, nsteps - 1, dt, eps, precision,
+                      sx + 3 * n, sv + 3 * n, 1, st));
+  }
+  const unsigned b3 = (unsigned)((3 * n + 255) / 256);
+  for (int64_t j = nsteps - 1; j >= 0; j--) {
+    adj_pre_kernel<<<b3, 256, 0, st>>>(sx + 3 * n * j, sv + 3 * n * j, n, dt, xbar, vbar, (double*)ws.xh.ptr,
+                                       (double*)ws.w.ptr, (double*)ws.lam.ptr);
+    GH_LAUNCH_CHECK();
+    GH_TRY(direct_vjp((const double*)ws.xh.ptr, mass, n, eps, (const double*)ws.lam.ptr, precision,
+                      (double*)ws.gpos.ptr, (double*)ws.gmass.ptr, st));
+    adj_post_kernel<<<b3, 256, 0, st>>>(n, dt, (const double*)ws.w.ptr, (const double*)ws.gpos.ptr,
+                                        (const double*)ws.gmass.ptr, xbar, vbar, mbar);
+    GH_LAUNCH_CHECK();
+  }
   return GH_OK;
 }
 

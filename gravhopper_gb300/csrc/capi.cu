@@ -65,7 +65,7 @@ static int host_call(HostKind kind, const double* pos, const double* mass, int64
     rc = direct_force((const double*)s->pos.ptr, (const double*)s->mass.ptr, np, dt, nt, eps,
                       precision, (double*)s->out.ptr, s->stream);
   else
-    rc = tree_force((const double*)s->pos.ptr, (const double*)s->mass.ptr, np, dt, nt, eps, theta,
+    rc = tree_force((const double*)s->pos.ptr, (const double*)s->mass.ptr, np, dt, nt, eps, theta, precision,
                     (double*)s->out.ptr, s->stream);
   if (rc != GH_OK) {
     cudaStreamSynchronize(s->stream);
@@ -107,9 +107,9 @@ int gh_tree_force_position(const double* pos, const double* mass, int64_t np, co
 }
 
 int gh_tree_dev(const double* pos, const double* mass, int64_t np, const double* force_pos, int64_t nf,
-                double eps, double theta, double* acc, void* stream) {
+                double eps, double theta, int precision, double* acc, void* stream) {
   clear_error();
-  return tree_force(pos, mass, np, force_pos, nf, eps, theta, acc, (cudaStream_t)stream);
+  return tree_force(pos, mass, np, force_pos, nf, eps, theta, precision, acc, (cudaStream_t)stream);
 }
 
 int gh_direct_host(const double* pos, const double* mass, int64_t np, const double* force_pos,
@@ -142,7 +142,7 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
   if (algorithm == GH_ALGO_DIRECT)
     return direct_run(pos, vel, mass, np, nsteps, dt, eps, precision, hist_pos, hist_vel,
                       hist_stride, st);
-  return tree_run(pos, vel, mass, np, nsteps, dt, eps, theta, hist_pos, hist_vel, hist_stride, st);
+  return tree_run(pos, vel, mass, np, nsteps, dt, eps, theta, precision, hist_pos, hist_vel, hist_stride, st);
 }
 
 int gh_ensemble_run(double* pos, double* vel, const double* mass, const int64_t* offsets, int64_t nsys,
@@ -159,6 +159,16 @@ int gh_direct_vjp_dev(const double* pos, const double* mass, int64_t np, double 
                       int precision, double* grad_pos, double* grad_mass, void* stream) {
   clear_error();
   return direct_vjp(pos, mass, np, eps, cot, precision, grad_pos, grad_mass, (cudaStream_t)stream);
+}
+
+int gh_dkd_backward_dev(const double* x0, const double* v0, const double* mass, int64_t np, int64_t nsteps,
+                        double dt, double eps, int precision, double* xbar, double* vbar, double* mbar,
+                        void* stream) {
+  clear_error();
+  if (precision != GH_PREC_FP64 && precision != GH_PREC_MIXED)
+    return set_error(GH_ERR_ARG, "unknown precision %d", precision);
+  if (!(eps >= 0.0)) return set_error(GH_ERR_ARG, "eps must be >= 0");
+  return dkd_backward(x0, v0, mass, np, nsteps, dt, eps, precision, xbar, vbar, mbar, (cudaStream_t)stream);
 }
 
 int gh_potential_dev(const double* pos, const double* mass, int64_t np, double eps, double* phi, void* stream) {

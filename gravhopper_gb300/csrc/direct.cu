@@ -98,8 +98,17 @@ struct DirectWS {
 static DirectWS g_ws[64];
 static std::recursive_mutex g_mu;
 
-// Shape of the mixed kernel used by this library (index into kMixedShapes).
-static int g_mixed_shape = 0;
+// Shape of the mixed kernel (index into kMixedShapes); -1 picks by problem size.
+static int g_mixed_shape = -1;
+
+// Measured on GB300 (pairs/s per shape at N = 2000, 16384, 1048576): small systems
+// want small tiles (more CTAs share the sources), large ones the widest CTAs.
+static int auto_shape(int64_t np, int64_t nt) {
+  const int64_t n = np > nt ? np : nt;
+  if (n >= (1 << 19)) return 4;  // 512 threads, 2 packs
+  if (n >= 8192) return 3;       // 128 threads, 2 packs, 4 CTAs/SM
+  return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
+}
 
 template <bool G, int T, int P, int B, class Epi>
 static int launch_shape(const StreamK& sk, const float4* src, int64_t np, const float4* tgt, int64_t nt,
@@ -128,7 +137,11 @@ static int dispatch_shape(int shape, const StreamK& sk, const float4* src, int64
     case 1: return launch_shape<G, 256, 4, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 2: return launch_shape<G, 128, 4, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 3: return launch_shape<G, 128, 2, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    default: return launch_shape<G, 512, 2, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 4: return launch_shape<G, 512, 2, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 5: return launch_shape<G, 256, 2, 3>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 6: return launch_shape<G, 128, 2, 6>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 7: return launch_shape<G, 256, 1, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    default: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
   }
 }
 
@@ -141,7 +154,11 @@ static int mixed_grid_cap(int num_sms, int shape, bool guard) {
       case 1: o = guard ? occupancy_shape<true, 256, 4, 1>() : occupancy_shape<false, 256, 4, 1>(); break;
       case 2: o = guard ? occupancy_shape<true, 128, 4, 2>() : occupancy_shape<false, 128, 4, 2>(); break;
       case 3: o = guard ? occupancy_shape<true, 128, 2, 4>() : occupancy_shape<false, 128, 2, 4>(); break;
-      default: o = guard ? occupancy_shape<true, 512, 2, 1>() : occupancy_shape<false, 512, 2, 1>(); break;
+      case 4: o = guard ? occupancy_shape<true, 512, 2, 1>() : occupancy_shape<false, 512, 2, 1>(); break;
+      case 5: o = guard ? occupancy_shape<true, 256, 2, 3>() : occupancy_shape<false, 256, 2, 3>(); break;
+      case 6: o = guard ? occupancy_shape<true, 128, 2, 6>() : occupancy_shape<false, 128, 2, 6>(); break;
+      case 7: o = guard ? occupancy_shape<true, 256, 1, 4>() : occupancy_shape<false, 256, 1, 4>(); break;
+      default: o = guard ? occupancy_shape<true, 512, 2, 2>() : occupancy_shape<false, 512, 2, 2>(); break;
     }
   }
   return o * num_sms;
@@ -158,7 +175,7 @@ StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap, int tile, int jt) {
 }
 
 int set_mixed_shape(int shape) {
-  if (shape < 0) shape = 0;
+  if (shape < 0) shape = -1;
   if (shape >= kNumMixedShapes) return set_error(GH_ERR_ARG, "mixed shape %d out of range", shape);
   g_mixed_shape = shape;
   return GH_OK;
@@ -197,7 +214,7 @@ static int launch_mixed(DirectWS& ws, const float4* src, int64_t np, const float
   GH_TRY(device_info(&di));
   const float eps2 = (float)(eps * eps);
   const bool guard = !(eps2 > 0.f);
-  const int shape = g_mixed_shape;
+  const int shape = g_mixed_shape >= 0 ? g_mixed_shape : auto_shape(np, nt);
   const MixedShape ms = kMixedShapes[shape];
   StreamK sk = mixed_plan(np, nt, mixed_grid_cap(di.num_sms, shape, guard), ms.threads * 2 * ms.packs,
                           ms.threads);

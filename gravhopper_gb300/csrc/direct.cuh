@@ -202,7 +202,8 @@ __global__ void __launch_bounds__(F64_THREADS)
 struct MixedShape {
   int threads, packs, minb;
 };
-constexpr MixedShape kMixedShapes[] = {{256, 2, 2}, {256, 4, 1}, {128, 4, 2}, {128, 2, 4}, {512, 2, 1}};
+constexpr MixedShape kMixedShapes[] = {{256, 2, 2}, {256, 4, 1}, {128, 4, 2}, {128, 2, 4}, {512, 2, 1},
+                                       {256, 2, 3}, {128, 2, 6}, {256, 1, 4}, {512, 2, 2}};
 constexpr int kNumMixedShapes = (int)(sizeof(kMixedShapes) / sizeof(kMixedShapes[0]));
 
 struct StreamK {
@@ -290,9 +291,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
   constexpr int R = 2 * P, TILE = THREADS * R, JT = THREADS;
   constexpr int64_t SLOT = mixed_slot_floats(THREADS, P);
   // Sources duplicated per lane pair: (x,x,y,y) and (z,z,m,m).
-  __shared__ __align__(16) float4 tile[2 * JT];
+  __shared__ __align__(16) float4 tile[2 * 2 * JT];
   __shared__ int s_last;
   const int tid = threadIdx.x;
+  int buf = 0;
   const int64_t g = blockIdx.x;
   const int64_t u_begin = sk_start(sk, g), u_end = sk_start(sk, g + 1);
   const f2 E2 = f2make(eps2, eps2);
@@ -321,17 +323,27 @@ __global__ void __launch_bounds__(THREADS, MINB)
       hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = 0ull;
     }
 
+    // Double-buffered chunks: the next chunk's source is loaded into a register while
+    // the current one is computed, and written to the other buffer afterwards, so one
+    // barrier per chunk suffices (the barrier of chunk c orders every read of the
+    // buffer it reuses, last read in chunk c-1).  Padding sources have zero mass at the
+    // origin: their terms are exactly 0.
+    float4 pre;
+    {
+      const int64_t j = c0 * JT + tid;
+      pre = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     for (int64_t c = c0; c < c1; c++) {
+      float4* tb = tile + buf * (2 * JT);
+      tb[2 * tid + 0] = make_float4(pre.x, pre.x, pre.y, pre.y);
+      tb[2 * tid + 1] = make_float4(pre.z, pre.z, pre.w, pre.w);
       __syncthreads();
-      {
-        const int64_t j = c * JT + tid;
-        // Padding sources have zero mass at the origin: their terms are exactly 0.
-        float4 s = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        tile[2 * tid + 0] = make_float4(s.x, s.x, s.y, s.y);
-        tile[2 * tid + 1] = make_float4(s.z, s.z, s.w, s.w);
+      if (c + 1 < c1) {
+        const int64_t j = (c + 1) * JT + tid;
+        pre = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      __syncthreads();
-      mixed_chunk<GUARD, P, JT>(tile, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      buf ^= 1;
     }
 
     const bool whole = (c0 == 0 && c1 == sk.chunks);

@@ -24,17 +24,22 @@ int drift_prepare_f64(const double* x, const double* v, int64_t n, double dt, do
 
 // Barnes-Hut acceleration in code units (tpos == nullptr: targets are the sources).
 int tree_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt,
-               double eps, double theta, double* acc, cudaStream_t st);
+               double eps, double theta, int precision, double* acc, cudaStream_t st);
 
 // `nsteps` leapfrog steps with the tree force (rebuilt every step).
 int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,
-             double eps, double theta, double* hist_x, double* hist_v, int64_t stride,
+             double eps, double theta, int precision, double* hist_x, double* hist_v, int64_t stride,
              cudaStream_t st);
 
 // VJP of the direct-sum acceleration (adjoint.cu): cotangent lam (N,3) -> gradients
 // with respect to positions (N,3) and masses (N, may be null).
 int direct_vjp(const double* pos, const double* mass, int64_t n, double eps, const double* lam, int precision,
                double* gpos, double* gmass, cudaStream_t st);
+
+// Reverse pass of nsteps direct-sum DKD steps starting from (x0, v0): recomputes the
+// states, then updates the cotangents (xbar, vbar) in place and adds to mbar.
+int dkd_backward(const double* x0, const double* v0, const double* mass, int64_t n, int64_t nsteps, double dt,
+                 double eps, int precision, double* xbar, double* vbar, double* mbar, cudaStream_t st);
 
 // Per-particle softened potential phi_k = -sum_{j != k} m_j / sqrt(r^2 + eps^2) (G=1).
 int potential(const double* pos, const double* mass, int64_t n, double eps, double* phi, cudaStream_t st);

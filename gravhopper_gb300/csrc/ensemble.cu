@@ -33,9 +33,10 @@ __global__ void __launch_bounds__(THREADS)
                          const int2* __restrict__ items, int n_items, int* __restrict__ counter) {
   constexpr int JT = THREADS;
   constexpr int TILE = THREADS * 2 * P;
-  __shared__ __align__(16) float4 tile[2 * JT];
+  __shared__ __align__(16) float4 tile[2 * 2 * JT];
   __shared__ int s_item;
   const int tid = threadIdx.x;
+  int buf = 0;
   for (;;) {
     if (tid == 0) s_item = atomicAdd(&counter[0], 1);
     __syncthreads();
@@ -60,16 +61,19 @@ __global__ void __launch_bounds__(THREADS)
       hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = 0ull;
     }
     const f2 E2 = f2make(S.eps2, S.eps2);
+    // Double-buffered source chunks with a register prefetch (see direct_mixed_kernel).
+    float4 pre = tid < S.n ? src[S.off + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
     for (int c0 = 0; c0 < S.n; c0 += JT) {
+      float4* tb = tile + buf * (2 * JT);
+      tb[2 * tid + 0] = make_float4(pre.x, pre.x, pre.y, pre.y);
+      tb[2 * tid + 1] = make_float4(pre.z, pre.z, pre.w, pre.w);
       __syncthreads();
-      {
-        const int j = c0 + tid;
-        float4 s = j < S.n ? src[S.off + j] : make_float4(0.f, 0.f, 0.f, 0.f);
-        tile[2 * tid + 0] = make_float4(s.x, s.x, s.y, s.y);
-        tile[2 * tid + 1] = make_float4(s.z, s.z, s.w, s.w);
+      if (c0 + JT < S.n) {
+        const int j = c0 + JT + tid;
+        pre = j < S.n ? src[S.off + j] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      __syncthreads();
-      mixed_chunk<GUARD, P, JT>(tile, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      buf ^= 1;
     }
     EpiDKD epi;
     epi.x = x;

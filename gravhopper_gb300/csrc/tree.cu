@@ -202,6 +202,8 @@ struct NodeArrays {
   dvec4* C;      // (cx, cy, cz, size)                    exact opening test
   dvec4* M;      // (comx, comy, comz, mass)              interaction
   dvec4* F;      // (first moment x, y, z, mass)          build only
+  float4* Mh;    // (comx_hi, comy_hi, comz_hi, mass)     mixed-precision interaction
+  float4* Ml;    // (comx_lo, comy_lo, comz_lo, 0)
   int* first;    // first particle (sorted position)
   int* level;
 };
@@ -293,6 +295,14 @@ __global__ void level_scatter_kernel(const int* __restrict__ level, int nnodes, 
 
 __device__ __forceinline__ int node_next(const float4* __restrict__ L, int k) { return __float_as_int(L[k].w); }
 
+// FP32 hi/lo split of a cell's centre of mass, for the mixed-precision walk.
+__device__ __forceinline__ void store_mixed_com(const NodeArrays& na, int k, double x, double y, double z,
+                                                double m) {
+  const float hx = (float)x, hy = (float)y, hz = (float)z;
+  na.Mh[k] = make_float4(hx, hy, hz, (float)m);
+  na.Ml[k] = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), 0.f);
+}
+
 __global__ void com_leaf_kernel(NodeArrays na, int nnodes, const uint32_t* __restrict__ perm,
                                 const double* __restrict__ pos, const double* __restrict__ mass) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -302,6 +312,7 @@ __global__ void com_leaf_kernel(NodeArrays na, int nnodes, const uint32_t* __res
   const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
   na.M[k] = make_dvec4(x, y, z, m);
   na.F[k] = make_dvec4(dmul(m, x), dmul(m, y), dmul(m, z), m);
+  store_mixed_com(na, k, x, y, z, m);
 }
 
 __global__ void com_level_kernel(NodeArrays na, const int* __restrict__ bucket, const int* __restrict__ off,
@@ -320,7 +331,9 @@ __global__ void com_level_kernel(NodeArrays na, const int* __restrict__ bucket, 
       m = dadd(m, f.w);
     }
     na.F[k] = make_dvec4(fx, fy, fz, m);
-    na.M[k] = make_dvec4(ddiv(fx, m), ddiv(fy, m), ddiv(fz, m), m);
+    const double cx = ddiv(fx, m), cy = ddiv(fy, m), cz = ddiv(fz, m);
+    na.M[k] = make_dvec4(cx, cy, cz, m);
+    store_mixed_com(na, k, cx, cy, cz, m);
   }
 }
 
@@ -341,12 +354,18 @@ __device__ __forceinline__ double rsqrt_f64(double s) {
   return y;
 }
 
-template <bool GUARD, class Epi>
+// MIXED: accepted cells interact in FP32 on hi/lo split coordinates (the
+// difference keeps ~2^-48 of |x|), partial sums folded into a two-sum (hi, lo)
+// accumulator every 32 interactions; otherwise FP64 with a Newton-refined rsqrt.
+// The opening decisions are the same exact ones in both forms.
+constexpr int TW_FOLD = 32;
+
+template <bool GUARD, bool MIXED, class Epi>
 __global__ void __launch_bounds__(TW_THREADS)
     tree_walk_kernel(const float4* __restrict__ nA, const float4* __restrict__ nL, const dvec4* __restrict__ nC,
-                     const dvec4* __restrict__ nM, int nnodes, const double* __restrict__ tpos,
-                     const uint32_t* __restrict__ order, int64_t nt, double eps2, double theta, float th2_lo,
-                     float th2_hi, Epi epi) {
+                     const dvec4* __restrict__ nM, const float4* __restrict__ nMh, const float4* __restrict__ nMl,
+                     int nnodes, const double* __restrict__ tpos, const uint32_t* __restrict__ order, int64_t nt,
+                     double eps2, double theta, float th2_lo, float th2_hi, Epi epi) {
   const int64_t slot = (int64_t)blockIdx.x * TW_THREADS + threadIdx.x;
   const bool valid = slot < nt;
   const int64_t t = valid ? (order ? (int64_t)order[slot] : slot) : 0;
@@ -360,7 +379,11 @@ __global__ void __launch_bounds__(TW_THREADS)
   const float l0 = f32_lo(p0, h0), l1 = f32_lo(p1, h1), l2 = f32_lo(p2, h2);
   // d^2 below this needs the exact test: FP32 differences lose too much relative to |x|
   const float near2 = 1e-18f * (h0 * h0 + h1 * h1 + h2 * h2);
+  const float eps2f = (float)eps2;
   double ax = 0.0, ay = 0.0, az = 0.0;
+  float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
+  float hx = 0.f, hy = 0.f, hz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;  // two-sum hi, lo
+  int pending = 0;
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
   while (node < nnodes) {
@@ -392,15 +415,44 @@ __global__ void __launch_bounds__(TW_THREADS)
         }
       }
       if (accept) {
-        const dvec4 M = nM[node];
-        const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
-        const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
-        if (!GUARD || s != 0.0) {
-          const double y = rsqrt_f64(s);
-          const double f = M.w * (y * (y * y));
-          ax = fma(f, dx, ax);
-          ay = fma(f, dy, ay);
-          az = fma(f, dz, az);
+        if (MIXED) {
+          const float4 H = nMh[node];
+          const float4 Q = nMl[node];
+          const float dx = (H.x - h0) + (Q.x - l0);
+          const float dy = (H.y - h1) + (Q.y - l1);
+          const float dz = (H.z - h2) + (Q.z - l2);
+          const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2f)));
+          float r = rsqrt_approx(s);
+          if (GUARD) r = s > 0.f ? r : 0.f;
+          const float f = H.w * (r * (r * r));
+          px = fmaf(f, dx, px);
+          py = fmaf(f, dy, py);
+          pz = fmaf(f, dz, pz);
+          if (++pending == TW_FOLD) {
+            float sx, ex;
+            two_sum(hx, px, sx, ex);
+            hx = sx;
+            qx += ex;
+            two_sum(hy, py, sx, ex);
+            hy = sx;
+            qy += ex;
+            two_sum(hz, pz, sx, ex);
+            hz = sx;
+            qz += ex;
+            px = py = pz = 0.f;
+            pending = 0;
+          }
+        } else {
+          const dvec4 M = nM[node];
+          const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
+          const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+          if (!GUARD || s != 0.0) {
+            const double y = rsqrt_f64(s);
+            const double f = M.w * (y * (y * y));
+            ax = fma(f, dx, ax);
+            ay = fma(f, dy, ay);
+            az = fma(f, dz, az);
+          }
         }
         skip = nx;
         lane_next = nx;
@@ -410,6 +462,11 @@ __global__ void __launch_bounds__(TW_THREADS)
     }
     node = __reduce_min_sync(0xffffffffu, lane_next);
   }
+  if (MIXED) {
+    ax = (double)hx + (double)qx + (double)px;
+    ay = (double)hy + (double)qy + (double)py;
+    az = (double)hz + (double)qz + (double)pz;
+  }
   if (valid) epi(t, ax, ay, az);
 }
 
@@ -418,7 +475,7 @@ __global__ void __launch_bounds__(TW_THREADS)
 // ---------------------------------------------------------------------------
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
-  Buffer nA, nL, nC, nM, nF, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
+  Buffer nA, nL, nC, nM, nF, nMh, nMl, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
   int* host_flags = nullptr;  // pinned: tie, maxdepth, nnodes
   int words = TREE_MIN_WORDS;
 };
@@ -432,6 +489,8 @@ static NodeArrays node_arrays(TreeWS& ws) {
   na.C = (dvec4*)ws.nC.ptr;
   na.M = (dvec4*)ws.nM.ptr;
   na.F = (dvec4*)ws.nF.ptr;
+  na.Mh = (float4*)ws.nMh.ptr;
+  na.Ml = (float4*)ws.nMl.ptr;
   na.first = (int*)ws.first.ptr;
   na.level = (int*)ws.level.ptr;
   return na;
@@ -505,6 +564,8 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nM, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nF, (size_t)nnodes * sizeof(dvec4)));
+  GH_TRY(ensure(ws.nMh, (size_t)nnodes * sizeof(float4)));
+  GH_TRY(ensure(ws.nMl, (size_t)nnodes * sizeof(float4)));
   GH_TRY(ensure(ws.first, (size_t)nnodes * sizeof(int)));
   GH_TRY(ensure(ws.level, (size_t)nnodes * sizeof(int)));
   NodeArrays na = node_arrays(ws);
@@ -537,9 +598,17 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   return GH_OK;
 }
 
+template <bool G, bool MX, class Epi>
+static void launch_walk(const NodeArrays& na, const BuiltTree& bt, const double* tpos, const uint32_t* order,
+                        int64_t nt, double eps2, double theta, float lo, float hi, const Epi& epi, cudaStream_t st) {
+  const unsigned blocks = (unsigned)((nt + TW_THREADS - 1) / TW_THREADS);
+  tree_walk_kernel<G, MX, Epi><<<blocks, TW_THREADS, 0, st>>>(na.A, na.L, na.C, na.M, na.Mh, na.Ml, bt.nnodes, tpos,
+                                                              order, nt, eps2, theta, lo, hi, epi);
+}
+
 template <class Epi>
 static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const uint32_t* order, int64_t nt,
-                     double eps, double theta, const Epi& epi, cudaStream_t st) {
+                     double eps, double theta, int precision, const Epi& epi, cudaStream_t st) {
   if (nt == 0) return GH_OK;
   const double eps2 = eps * eps;
   float lo = -1.f, hi = -1.f;  // theta <= 0 or NaN: never open by the prefilter, never accept
@@ -547,29 +616,37 @@ static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const 
     lo = (float)(theta * theta * (1.0 - TREE_MARGIN));
     hi = (float)(theta * theta * (1.0 + TREE_MARGIN));
   }
-  const unsigned blocks = (unsigned)((nt + TW_THREADS - 1) / TW_THREADS);
   NodeArrays na = node_arrays(ws);
+  const bool mixed = precision == GH_PREC_MIXED;
+  const bool guard = mixed ? !((float)eps2 > 0.f) : eps2 == 0.0;
   prof_begin(st);
-  if (eps2 == 0.0)
-    tree_walk_kernel<true, Epi><<<blocks, TW_THREADS, 0, st>>>(na.A, na.L, na.C, na.M, bt.nnodes, tpos, order, nt,
-                                                               eps2, theta, lo, hi, epi);
-  else
-    tree_walk_kernel<false, Epi><<<blocks, TW_THREADS, 0, st>>>(na.A, na.L, na.C, na.M, bt.nnodes, tpos, order,
-                                                                nt, eps2, theta, lo, hi, epi);
+  if (mixed) {
+    if (guard)
+      launch_walk<true, true>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+    else
+      launch_walk<false, true>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+  } else {
+    if (guard)
+      launch_walk<true, false>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+    else
+      launch_walk<false, false>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+  }
   prof_end(st);
   GH_LAUNCH_CHECK();
   return GH_OK;
 }
 
-static int check_tree_args(int64_t np, int64_t nt, double eps) {
+static int check_tree_args(int64_t np, int64_t nt, double eps, int precision) {
   if (np < 0 || nt < 0) return set_error(GH_ERR_ARG, "negative particle count");
+  if (precision != GH_PREC_FP64 && precision != GH_PREC_MIXED)
+    return set_error(GH_ERR_ARG, "unknown precision %d", precision);
   if (!(eps >= 0.0)) return set_error(GH_ERR_ARG, "eps must be >= 0 (got %g)", eps);
   return GH_OK;
 }
 
 int tree_force(const double* pos, const double* mass, int64_t np, const double* tpos, int64_t nt, double eps,
-               double theta, double* acc, cudaStream_t st) {
-  GH_TRY(check_tree_args(np, nt, eps));
+               double theta, int precision, double* acc, cudaStream_t st) {
+  GH_TRY(check_tree_args(np, nt, eps, precision));
   const bool self = (tpos == nullptr);
   if (self) nt = np;
   if (nt == 0) return GH_OK;
@@ -584,13 +661,13 @@ int tree_force(const double* pos, const double* mass, int64_t np, const double* 
   BuiltTree bt;
   GH_TRY(tree_build(ws, pos, mass, np, eps, st, &bt));
   EpiStore epi{acc};
-  if (self) return tree_walk(ws, bt, pos, (const uint32_t*)ws.idx.ptr, np, eps, theta, epi, st);
-  return tree_walk(ws, bt, tpos, nullptr, nt, eps, theta, epi, st);
+  if (self) return tree_walk(ws, bt, pos, (const uint32_t*)ws.idx.ptr, np, eps, theta, precision, epi, st);
+  return tree_walk(ws, bt, tpos, nullptr, nt, eps, theta, precision, epi, st);
 }
 
 int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt, double eps,
-             double theta, double* hist_x, double* hist_v, int64_t stride, cudaStream_t st) {
-  GH_TRY(check_tree_args(np, 0, eps));
+             double theta, int precision, double* hist_x, double* hist_v, int64_t stride, cudaStream_t st) {
+  GH_TRY(check_tree_args(np, 0, eps, precision));
   std::lock_guard<std::recursive_mutex> lk(g_tree_mu);
   DeviceInfo di;
   GH_TRY(device_info(&di));
@@ -617,7 +694,7 @@ int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nstep
       epi.hist_x = hist_x + slot * np * 3;
       epi.hist_v = hist_v + slot * np * 3;
     }
-    GH_TRY(tree_walk(ws, bt, xh, (const uint32_t*)ws.idx.ptr, np, eps, theta, epi, st));
+    GH_TRY(tree_walk(ws, bt, xh, (const uint32_t*)ws.idx.ptr, np, eps, theta, precision, epi, st));
   }
   return GH_OK;
 }

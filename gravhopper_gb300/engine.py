@@ -37,8 +37,10 @@ def direct_force(pos, mass, eps, force_pos=None, precision="fp64", out=None, str
     return out
 
 
-def tree_force(pos, mass, eps, theta=0.7, force_pos=None, out=None, stream=None):
-    """Barnes-Hut acceleration (code units), FP64, reference opening criterion."""
+def tree_force(pos, mass, eps, theta=0.7, force_pos=None, out=None, stream=None, precision="fp64"):
+    """Barnes-Hut acceleration (code units) with the reference's opening decisions.
+
+    ``precision='mixed'`` evaluates accepted cells in FP32 (compensated sums)."""
     _check(pos, "pos", 3)
     _check(mass, "mass")
     if mass.shape[0] != pos.shape[0]:
@@ -50,7 +52,7 @@ def tree_force(pos, mass, eps, theta=0.7, force_pos=None, out=None, stream=None)
         out = torch.empty((n_out, 3), dtype=torch.float64, device=pos.device)
     _capi.call("gh_tree_dev", _capi.ptr(pos), _capi.ptr(mass), pos.shape[0], _capi.ptr(force_pos),
                0 if force_pos is None else force_pos.shape[0], float(eps), float(theta),
-               _capi.ptr(out), _capi.stream_handle(stream))
+               _capi.PRECISIONS[precision], _capi.ptr(out), _capi.stream_handle(stream))
     return out
 
 

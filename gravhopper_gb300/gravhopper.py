@@ -127,7 +127,9 @@ class Simulation(object):
         return self.params["theta"]
 
     def set_precision(self, precision):
-        """'fp64' (reference arithmetic) or 'mixed' (FP32 pairs, direct sum only)."""
+        """'fp64' (reference arithmetic) or 'mixed' (FP32 pair arithmetic with compensated
+        sums; for the tree, the accepted cells' interactions, with the same opening
+        decisions).  State and integration stay FP64 either way."""
         if precision not in ("fp64", "mixed"):
             raise ValueError("precision must be 'fp64' or 'mixed'.")
         self.params["precision"] = precision

@@ -88,14 +88,16 @@ int gh_direct_host(const double* pos, const double* mass, int64_t np, const doub
 int gh_direct_dev(const double* pos, const double* mass, int64_t np, const double* force_pos,
                   int64_t nf, double eps, int precision, double* acc, void* stream);
 
-/* Barnes-Hut acceleration (code units) into acc (nf,3), or (np,3) when force_pos == NULL. */
+/* Barnes-Hut acceleration (code units) into acc (nf,3), or (np,3) when force_pos == NULL.
+ * Opening decisions are the reference's in both precisions; GH_PREC_MIXED evaluates the
+ * accepted cells' monopoles in FP32 on hi/lo split coordinates with compensated sums. */
 int gh_tree_dev(const double* pos, const double* mass, int64_t np, const double* force_pos, int64_t nf,
-                double eps, double theta, double* acc, void* stream);
+                double eps, double theta, int precision, double* acc, void* stream);
 
 /* Advances (pos, vel) in place by nsteps drift-kick-drift leapfrog steps
  * (Simulation.perform_timestep, gravhopper/gravhopper.py:405-416): pos [kpc],
  * vel [km/s], mass [Msun], dt [Myr], eps [kpc].  algorithm GH_ALGO_DIRECT uses
- * `precision`; GH_ALGO_TREE uses `theta` (FP64 walk).  When hist_pos/hist_vel are
+ * `precision`; GH_ALGO_TREE uses `theta` and `precision` (the walk's interactions).  When hist_pos/hist_vel are
  * non-NULL, the state after every hist_stride-th step is written to consecutive
  * (np,3) slots of them (nsteps/hist_stride slots). */
 int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t nsteps,
@@ -117,8 +119,9 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
 int gh_direct_mixed_noalloc(const double* pos, const double* mass, int64_t np, double eps, double* acc,
                             void* stream);
 
-/* Selects the tile shape of the mixed-precision direct kernel (0 .. gh_direct_num_shapes()-1;
- * default 0) for all later calls in this process (no counterpart in the reference). */
+/* Selects the tile shape of the mixed-precision direct kernel (0 .. gh_direct_num_shapes()-1)
+ * for all later calls in this process; -1 (the default) picks the shape by problem size.
+ * No counterpart in the reference. */
 int gh_direct_set_shape(int shape);
 int gh_direct_num_shapes(void);
 
@@ -130,6 +133,16 @@ int gh_direct_num_shapes(void);
  * grad_mass (np) = sum_i cot_i . da_i/dm.  precision GH_PREC_FP64 or GH_PREC_MIXED. */
 int gh_direct_vjp_dev(const double* pos, const double* mass, int64_t np, double eps, const double* cot,
                       int precision, double* grad_pos, double* grad_mass, void* stream);
+
+/* Reverse-mode pass through nsteps direct-sum drift-kick-drift steps that start from
+ * the state (x0, v0) (device buffers; same units as gh_run_dkd).  Recomputes the
+ * nsteps states from (x0, v0), then back-propagates: on entry (xbar, vbar) hold the
+ * cotangents of the state after the last step, on return those of (x0, v0); mbar,
+ * when non-NULL, is incremented by the mass gradient.  One checkpoint segment of a
+ * differentiable rollout. */
+int gh_dkd_backward_dev(const double* x0, const double* v0, const double* mass, int64_t np, int64_t nsteps,
+                        double dt, double eps, int precision, double* xbar, double* vbar, double* mbar,
+                        void* stream);
 
 /* Per-particle softened potential phi (np) = -sum_{j != k} m_j / sqrt(r^2 + eps^2), code
  * units (G=1), FP64.  Potential energy = 0.5 * G * sum_k m_k phi_k. */

@@ -85,3 +85,28 @@ def test_single_particle_and_empty_runs(lib, cuda):
                                   0.1, 0.0, 3)
     np.testing.assert_array_equal(x.cpu().numpy(), ref_x)
     np.testing.assert_array_equal(v.cpu().numpy(), ref_v)
+
+
+def test_simulation_with_external_force_matches_restatement(golden, lib, cuda):
+    """Registered external forces run on the host each step (gravhopper.py:462-473);
+    the N-body part still comes from the GPU.  Same arithmetic as the restatement."""
+    import gravhopper_gb300 as gh
+    n = 300
+    pos0, vel0, mass = golden["plummer_pos"][:n], golden["plummer_vel"][:n], golden["plummer_mass"][:n]
+    centre = np.array([2e-3, 0.0, 0.0])
+
+    def pull(pos, args):  # km/s/Myr toward a fixed point, linear in distance
+        return -args["k"] * (np.asarray(pos) - centre)
+
+    sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct")
+    sim.add_IC({"pos": pos0, "vel": vel0, "mass": mass})
+    sim.add_external_force(pull, {"k": 50.0})
+    sim.run(6)
+    x, v = pos0.copy(), vel0.copy()
+    for _ in range(6):
+        xh = x + ((0.5 * v) * 0.005) * oracle.KMS_MYR_TO_KPC
+        acc = oracle.direct_summation(xh, mass, 5e-5) * oracle.ACCEL_UNIT + pull(xh, {"k": 50.0})
+        v = v + acc * 0.005
+        x = xh + ((0.5 * v) * 0.005) * oracle.KMS_MYR_TO_KPC
+    np.testing.assert_array_equal(sim.positions[6], x)
+    np.testing.assert_array_equal(sim.velocities[6], v)

@@ -98,6 +98,50 @@ def test_tree_run_matches_reference_trajectory(golden, lib, cuda):
     np.testing.assert_allclose(v.cpu().numpy(), golden["traj_tree_v_20"], rtol=1e-9, atol=1e-9)
 
 
+MIXED_TREE_RMS_TOL = 1e-6
+MIXED_TREE_MAX_TOL = 1e-3
+
+
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_mixed_tree_against_reference_golden(golden, lib, cuda, theta):
+    """Mixed walk: same opening decisions, FP32 interactions with compensated sums."""
+    import torch
+
+    from gravhopper_gb300 import engine
+    key = str(theta).replace(".", "p")
+    for pos, mass, eps, ref in ((golden["tree_pos"], golden["tree_mass"], 5e-5, golden[f"tree_{key}_out"]),
+                                (golden["hq_pos"], golden["hq_mass"], 0.1, golden[f"hq_{key}_out"])):
+        x = torch.from_numpy(pos).to(cuda)
+        m = torch.from_numpy(mass).to(cuda)
+        got = engine.tree_force(x, m, eps, theta, precision="mixed").cpu().numpy()
+        check(got, ref, MIXED_TREE_RMS_TOL, MIXED_TREE_MAX_TOL)
+
+
+def test_mixed_tree_large_against_oracle(lib, cuda):
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    ic = ics.hernquist_disk(200000, seed=9)
+    x = torch.from_numpy(ic["pos"]).to(cuda)
+    m = torch.from_numpy(ic["mass"]).to(cuda)
+    idx = np.random.default_rng(0).choice(200000, size=3000, replace=False)
+    got = engine.tree_force(x, m, 0.1, 0.7, precision="mixed").cpu().numpy()[idx]
+    ref = oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx], 0.1, 0.7)
+    check(got, ref, MIXED_TREE_RMS_TOL, MIXED_TREE_MAX_TOL)
+
+
+def test_mixed_tree_run_tracks_reference(golden, lib, cuda):
+    import torch
+
+    from gravhopper_gb300 import engine
+    x = torch.from_numpy(golden["plummer_pos"].copy()).to(cuda)
+    v = torch.from_numpy(golden["plummer_vel"].copy()).to(cuda)
+    m = torch.from_numpy(golden["plummer_mass"].copy()).to(cuda)
+    engine.run_dkd(x, v, m, 20, 0.005, 5e-5, algorithm="tree", precision="mixed", theta=0.7)
+    # close pairs amplify FP32 force errors over 20 steps (2 of 6000 coordinates > 1e-9 kpc)
+    np.testing.assert_allclose(x.cpu().numpy(), golden["traj_tree_x_20"], rtol=0, atol=1e-8)
+
+
 def test_simulation_default_tree(golden, lib, cuda):
     import gravhopper_gb300 as gh
     sim = gh.Simulation(dt=0.005, eps=5e-5)  # algorithm='tree' by default, theta 0.7
