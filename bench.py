@@ -350,18 +350,21 @@ def measure_tree(dev, n=1 << 20, steps=2):
     m = torch.from_numpy(ic["mass"]).to(dev)
     out = {"n": n, "workload": "Hernquist (70%) + exponential disk (30%), 1e11 Msun, eps=0.1 kpc, dt=0.5 Myr"}
     for theta in (0.7, 0.5):
-        x = torch.from_numpy(ic["pos"]).to(dev)
-        v = torch.from_numpy(ic["vel"]).to(dev)
-        engine.run_dkd(x, v, m, 1, 0.5, 0.1, algorithm="tree", theta=theta)
-        _capi.kernel_timing_collect()
-        _capi.kernel_timing(True)
-        t = _timed(lambda: engine.run_dkd(x, v, m, steps, 0.5, 0.1, algorithm="tree", theta=theta))
-        _capi.kernel_timing(False)
-        walk_ms, walks = _capi.kernel_timing_collect()
         key = f"theta_{theta}"
-        out[key] = {"particle_steps_per_s": n * steps / t, "ms_per_step": t / steps * 1e3,
-                    "walk_ms_per_step": walk_ms / max(walks, 1), "build_ms_per_step": t / steps * 1e3 -
-                    walk_ms / max(walks, 1)}
+        out[key] = {}
+        for prec in ("mixed", "fp64"):
+            x = torch.from_numpy(ic["pos"]).to(dev)
+            v = torch.from_numpy(ic["vel"]).to(dev)
+            engine.run_dkd(x, v, m, 1, 0.5, 0.1, algorithm="tree", theta=theta, precision=prec)
+            _capi.kernel_timing_collect()
+            _capi.kernel_timing(True)
+            t = _timed(lambda: engine.run_dkd(x, v, m, steps, 0.5, 0.1, algorithm="tree", theta=theta,
+                                              precision=prec))
+            _capi.kernel_timing(False)
+            walk_ms, walks = _capi.kernel_timing_collect()
+            out[key][prec] = {"particle_steps_per_s": n * steps / t, "ms_per_step": t / steps * 1e3,
+                              "walk_ms_per_step": walk_ms / max(walks, 1),
+                              "build_ms_per_step": t / steps * 1e3 - walk_ms / max(walks, 1)}
     # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
     # full serial build plus the walk of 2048 targets, scaled to all N targets.
     rng = np.random.default_rng(0)
