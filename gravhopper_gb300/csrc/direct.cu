@@ -110,18 +110,18 @@ static int auto_shape(int64_t np, int64_t nt) {
   return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
 }
 
-template <bool G, int T, int P, int B, class Epi>
+template <bool G, int T, int P, int B, class Epi, bool PK = true>
 static int launch_shape(const StreamK& sk, const float4* src, int64_t np, const float4* tgt, int64_t nt,
                         float eps2, float* partials, int* counters, const Epi& epi, cudaStream_t st) {
-  direct_mixed_kernel<G, T, P, B, Epi><<<(unsigned)sk.grid, T, 0, st>>>(src, np, tgt, nt, eps2, sk, partials,
-                                                                        counters, epi);
+  direct_mixed_kernel<G, T, P, B, Epi, PK><<<(unsigned)sk.grid, T, 0, st>>>(src, np, tgt, nt, eps2, sk, partials,
+                                                                            counters, epi);
   return GH_OK;
 }
 
-template <bool G, int T, int P, int B>
+template <bool G, int T, int P, int B, bool PK = true>
 static int occupancy_shape() {
   int o = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<G, T, P, B, EpiStore>, T, 0) !=
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<G, T, P, B, EpiStore, PK>, T, 0) !=
           cudaSuccess ||
       o < 1)
     o = 1;
@@ -141,7 +141,9 @@ static int dispatch_shape(int shape, const StreamK& sk, const float4* src, int64
     case 5: return launch_shape<G, 256, 2, 3>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 6: return launch_shape<G, 128, 2, 6>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 7: return launch_shape<G, 256, 1, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    default: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 8: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 9: return launch_shape<G, 256, 2, 2, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    default: return launch_shape<G, 512, 2, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
   }
 }
 
@@ -158,7 +160,10 @@ static int mixed_grid_cap(int num_sms, int shape, bool guard) {
       case 5: o = guard ? occupancy_shape<true, 256, 2, 3>() : occupancy_shape<false, 256, 2, 3>(); break;
       case 6: o = guard ? occupancy_shape<true, 128, 2, 6>() : occupancy_shape<false, 128, 2, 6>(); break;
       case 7: o = guard ? occupancy_shape<true, 256, 1, 4>() : occupancy_shape<false, 256, 1, 4>(); break;
-      default: o = guard ? occupancy_shape<true, 512, 2, 2>() : occupancy_shape<false, 512, 2, 2>(); break;
+      case 8: o = guard ? occupancy_shape<true, 512, 2, 2>() : occupancy_shape<false, 512, 2, 2>(); break;
+      case 9: o = guard ? occupancy_shape<true, 256, 2, 2, false>() : occupancy_shape<false, 256, 2, 2, false>(); break;
+      default: o = guard ? occupancy_shape<true, 512, 2, 1, false>() : occupancy_shape<false, 512, 2, 1, false>();
+        break;
     }
   }
   return o * num_sms;

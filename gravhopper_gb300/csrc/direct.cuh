@@ -203,7 +203,8 @@ struct MixedShape {
   int threads, packs, minb;
 };
 constexpr MixedShape kMixedShapes[] = {{256, 2, 2}, {256, 4, 1}, {128, 4, 2}, {128, 2, 4}, {512, 2, 1},
-                                       {256, 2, 3}, {128, 2, 6}, {256, 1, 4}, {512, 2, 2}};
+                                       {256, 2, 3}, {128, 2, 6}, {256, 1, 4}, {512, 2, 2},
+                                       {256, 2, 2}, {512, 2, 1}};  // last two: scalar FP32 loop
 constexpr int kNumMixedShapes = (int)(sizeof(kMixedShapes) / sizeof(kMixedShapes[0]));
 
 struct StreamK {
@@ -277,13 +278,62 @@ __device__ __forceinline__ void mixed_chunk(const float4* __restrict__ tile, con
   }
 }
 
+// The same chunk with scalar FP32 instructions (one target per instruction), for
+// comparison with the packed form on the same data layout.
+template <bool GUARD, int P, int JT>
+__device__ __forceinline__ void mixed_chunk_scalar(const float4* __restrict__ tile, const f2* tx, const f2* ty,
+                                                   const f2* tz, f2 E2, f2* hx, f2* hy, f2* hz, f2* lx, f2* ly,
+                                                   f2* lz) {
+  constexpr int R = 2 * P;
+  float sx[R], sy[R], sz[R], ax[R], ay[R], az[R];
+#pragma unroll
+  for (int p = 0; p < P; p++) {
+    f2split(tx[p], sx[2 * p], sx[2 * p + 1]);
+    f2split(ty[p], sy[2 * p], sy[2 * p + 1]);
+    f2split(tz[p], sz[2 * p], sz[2 * p + 1]);
+  }
+  float e2, e2b;
+  f2split(E2, e2, e2b);
+#pragma unroll
+  for (int r = 0; r < R; r++) ax[r] = ay[r] = az[r] = 0.f;
+#pragma unroll 4
+  for (int k = 0; k < JT; k++) {
+    const float4 a = tile[2 * k + 0];
+    const float4 b = tile[2 * k + 1];
+#pragma unroll
+    for (int r = 0; r < R; r++) {
+      const float dx = a.x - sx[r], dy = a.z - sy[r], dz = b.x - sz[r];
+      const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, e2)));
+      float ri = rsqrt_approx(r2);
+      if (GUARD) ri = r2 > 0.f ? ri : 0.f;
+      const float sc = (b.z * ri) * (ri * ri);
+      ax[r] = fmaf(sc, dx, ax[r]);
+      ay[r] = fmaf(sc, dy, ay[r]);
+      az[r] = fmaf(sc, dz, az[r]);
+    }
+  }
+#pragma unroll
+  for (int p = 0; p < P; p++) {
+    f2 s, e;
+    f2two_sum(hx[p], f2make(ax[2 * p], ax[2 * p + 1]), s, e);
+    hx[p] = s;
+    lx[p] = f2add(lx[p], e);
+    f2two_sum(hy[p], f2make(ay[2 * p], ay[2 * p + 1]), s, e);
+    hy[p] = s;
+    ly[p] = f2add(ly[p], e);
+    f2two_sum(hz[p], f2make(az[2 * p], az[2 * p + 1]), s, e);
+    hz[p] = s;
+    lz[p] = f2add(lz[p], e);
+  }
+}
+
 // Per-CTA scratch for split tiles: 2 slots (first and last tile of its range),
 // each 6 floats (hi/lo for x, y, z) per target of a tile.
 __host__ __device__ constexpr int64_t mixed_slot_floats(int threads, int packs) {
   return (int64_t)6 * threads * 2 * packs;
 }
 
-template <bool GUARD, int THREADS, int P, int MINB, class Epi>
+template <bool GUARD, int THREADS, int P, int MINB, class Epi, bool PACKED = true>
 __global__ void __launch_bounds__(THREADS, MINB)
     direct_mixed_kernel(const float4* __restrict__ src, int64_t np, const float4* __restrict__ tgt,
                         int64_t nt, float eps2, StreamK sk, float* __restrict__ partials,
@@ -342,7 +392,10 @@ __global__ void __launch_bounds__(THREADS, MINB)
         const int64_t j = (c + 1) * JT + tid;
         pre = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      if (PACKED)
+        mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      else
+        mixed_chunk_scalar<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
       buf ^= 1;
     }
 

@@ -61,22 +61,6 @@ __global__ void __launch_bounds__(RS_THREADS)
   hist[(int64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
 }
 
-// In-place exclusive scan of m entries by one 1024-thread block.
-__global__ void __launch_bounds__(1024) scan_u32_single_block(uint32_t* __restrict__ a, int64_t m) {
-  const int64_t per = (m + 1023) / 1024;
-  const int64_t b0 = threadIdx.x * per;
-  const int64_t b1 = b0 + per < m ? b0 + per : m;
-  int64_t s = 0;
-  for (int64_t i = b0; i < b1; i++) s += a[i];
-  int64_t total;
-  int64_t pre = block_exclusive_scan_1024(s, &total);
-  for (int64_t i = b0; i < b1; i++) {
-    uint32_t v = a[i];
-    a[i] = (uint32_t)pre;
-    pre += v;
-  }
-}
-
 __global__ void __launch_bounds__(RS_THREADS)
     rs_scatter_kernel(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ iin,
                       uint64_t* __restrict__ kout, uint32_t* __restrict__ iout, int words, int64_t n,
@@ -125,9 +109,12 @@ __global__ void __launch_bounds__(RS_THREADS)
   }
 }
 
+// Scratch layout: the digit-major histogram table (RS_BINS * nb + 1 entries, scanned
+// in place) followed by the multi-block scan's tile sums.
 int64_t radix_scratch_words(int64_t n) {
   const int64_t nb = (n + RS_TILE - 1) / RS_TILE;
-  return (int64_t)RS_BINS * (nb > 0 ? nb : 1);
+  const int64_t m = (int64_t)RS_BINS * (nb > 0 ? nb : 1);
+  return m + 1 + scan_scratch_ints(m);
 }
 
 int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t* idx_tmp, int words,
@@ -142,8 +129,11 @@ int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t*
       const int shift = 8 * p;
       rs_hist_kernel<<<nb, RS_THREADS, 0, st>>>(ks + (int64_t)w * n, n, shift, scratch_u32, nb);
       GH_LAUNCH_CHECK();
-      scan_u32_single_block<<<1, 1024, 0, st>>>(scratch_u32, (int64_t)RS_BINS * nb);
-      GH_LAUNCH_CHECK();
+      {
+        const int64_t m = (int64_t)RS_BINS * nb;
+        int* table = (int*)scratch_u32;
+        GH_TRY(exclusive_scan_i32(table, table, m, table + m + 1, st));
+      }
       rs_scatter_kernel<<<nb, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, scratch_u32, nb);
       GH_LAUNCH_CHECK();
       uint64_t* tk = ks;

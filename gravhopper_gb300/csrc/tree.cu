@@ -129,22 +129,34 @@ __global__ void root_kernel(const double* __restrict__ part, int nb, double eps,
 // ---------------------------------------------------------------------------
 // 2. Octant keys
 // ---------------------------------------------------------------------------
+constexpr int TREE_MAX_LEVELS = KEY_LEVELS * TREE_MAX_WORDS;
+
 __global__ void keys_kernel(const double* __restrict__ pos, int64_t n, const TreeRoot* __restrict__ root,
                             int words, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
+  // Child-centre offsets per level, the same for every particle: 0.5 * halfsize,
+  // halfsize halving each level (exact scalings of the root size).
+  __shared__ double offs[TREE_MAX_LEVELS];
+  if (threadIdx.x == 0) {
+    double hs = dmul(0.5, root->size);
+    for (int l = 0; l < words * KEY_LEVELS; l++) {
+      offs[l] = dmul(0.5, hs);
+      hs = dmul(0.5, hs);
+    }
+  }
+  __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const double p0 = pos[3 * i], p1 = pos[3 * i + 1], p2 = pos[3 * i + 2];
   double c0 = root->c[0], c1 = root->c[1], c2 = root->c[2];
-  double hs = dmul(0.5, root->size);
   for (int w = 0; w < words; w++) {
     uint64_t k = 0;
+#pragma unroll 3
     for (int l = 0; l < KEY_LEVELS; l++) {
-      const double off = dmul(0.5, hs);
+      const double off = offs[w * KEY_LEVELS + l];
       const unsigned g0 = p0 > c0, g1 = p1 > c1, g2 = p2 > c2;
       c0 = g0 ? dadd(c0, off) : dsub(c0, off);
       c1 = g1 ? dadd(c1, off) : dsub(c1, off);
       c2 = g2 ? dadd(c2, off) : dsub(c2, off);
-      hs = dmul(0.5, hs);
       k = (k << 3) | (uint64_t)(g0 | (g1 << 1) | (g2 << 2));
     }
     keys[(int64_t)w * n + i] = k;
@@ -269,9 +281,19 @@ __global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64
 // ---------------------------------------------------------------------------
 // 5. Monopole pass, deepest level first
 // ---------------------------------------------------------------------------
+// Warp-aggregated: lanes with the same level add once per warp (a few dozen levels
+// would otherwise serialise a million atomics on a few addresses).
+__device__ __forceinline__ unsigned lanemask_lt_tree() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
 __global__ void level_hist_kernel(const int* __restrict__ level, int nnodes, int* __restrict__ hist) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < nnodes) atomicAdd(&hist[level[k]], 1);
+  const int l = k < nnodes ? level[k] : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, l);
+  if (l >= 0 && (peers & lanemask_lt_tree()) == 0) atomicAdd(&hist[l], __popc(peers));
 }
 
 // hist (levels+1 entries) -> off (exclusive prefix) and cursor (= off)
@@ -290,7 +312,14 @@ __global__ void level_scan_kernel(const int* __restrict__ hist, int levels, int*
 __global__ void level_scatter_kernel(const int* __restrict__ level, int nnodes, int* __restrict__ cursor,
                                      int* __restrict__ bucket) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < nnodes) bucket[atomicAdd(&cursor[level[k]], 1)] = k;
+  const int l = k < nnodes ? level[k] : -1;
+  const unsigned peers = __match_any_sync(0xffffffffu, l);
+  const int leader = __ffs(peers) - 1;
+  const int rank = __popc(peers & lanemask_lt_tree());
+  int base = 0;
+  if (l >= 0 && rank == 0) base = atomicAdd(&cursor[l], __popc(peers));
+  base = __shfl_sync(0xffffffffu, base, leader);
+  if (l >= 0) bucket[base + rank] = k;
 }
 
 __device__ __forceinline__ int node_next(const float4* __restrict__ L, int k) { return __float_as_int(L[k].w); }
