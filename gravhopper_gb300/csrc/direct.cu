@@ -105,7 +105,7 @@ static int g_mixed_shape = -1;
 // want small tiles (more CTAs share the sources), large ones the widest CTAs.
 static int auto_shape(int64_t np, int64_t nt) {
   const int64_t n = np > nt ? np : nt;
-  if (n >= (1 << 19)) return 4;  // 512 threads, 2 packs
+  if (n >= (1 << 19)) return 10;  // 512 threads, 4 targets, scalar FP32 loop
   if (n >= 8192) return 3;       // 128 threads, 2 packs, 4 CTAs/SM
   return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
 }
@@ -143,7 +143,9 @@ static int dispatch_shape(int shape, const StreamK& sk, const float4* src, int64
     case 7: return launch_shape<G, 256, 1, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 8: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 9: return launch_shape<G, 256, 2, 2, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    default: return launch_shape<G, 512, 2, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 10: return launch_shape<G, 512, 2, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 11: return launch_shape<G, 256, 4, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    default: return launch_shape<G, 384, 3, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
   }
 }
 
@@ -162,7 +164,14 @@ static int mixed_grid_cap(int num_sms, int shape, bool guard) {
       case 7: o = guard ? occupancy_shape<true, 256, 1, 4>() : occupancy_shape<false, 256, 1, 4>(); break;
       case 8: o = guard ? occupancy_shape<true, 512, 2, 2>() : occupancy_shape<false, 512, 2, 2>(); break;
       case 9: o = guard ? occupancy_shape<true, 256, 2, 2, false>() : occupancy_shape<false, 256, 2, 2, false>(); break;
-      default: o = guard ? occupancy_shape<true, 512, 2, 1, false>() : occupancy_shape<false, 512, 2, 1, false>();
+      case 10:
+        o = guard ? occupancy_shape<true, 512, 2, 1, false>() : occupancy_shape<false, 512, 2, 1, false>();
+        break;
+      case 11:
+        o = guard ? occupancy_shape<true, 256, 4, 1, false>() : occupancy_shape<false, 256, 4, 1, false>();
+        break;
+      default:
+        o = guard ? occupancy_shape<true, 384, 3, 1, false>() : occupancy_shape<false, 384, 3, 1, false>();
         break;
     }
   }

@@ -204,7 +204,8 @@ struct MixedShape {
 };
 constexpr MixedShape kMixedShapes[] = {{256, 2, 2}, {256, 4, 1}, {128, 4, 2}, {128, 2, 4}, {512, 2, 1},
                                        {256, 2, 3}, {128, 2, 6}, {256, 1, 4}, {512, 2, 2},
-                                       {256, 2, 2}, {512, 2, 1}};  // last two: scalar FP32 loop
+                                       {256, 2, 2}, {512, 2, 1}, {256, 4, 1}, {384, 3, 1}};
+// Shapes 9-12 run the scalar FP32 loop (mixed_chunk_scalar); 0-8 the packed f32x2 loop.
 constexpr int kNumMixedShapes = (int)(sizeof(kMixedShapes) / sizeof(kMixedShapes[0]));
 
 struct StreamK {
