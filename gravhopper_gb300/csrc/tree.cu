@@ -208,14 +208,19 @@ __global__ void count_kernel(const int* __restrict__ lp, int64_t n, int* __restr
 // ---------------------------------------------------------------------------
 // 4. Nodes in preorder
 // ---------------------------------------------------------------------------
+// The walk's per-node record: one 64-byte line read per visited cell.
+struct __align__(64) WalkRec {
+  float4 A;   // (cx_hi, cy_hi, cz_hi, size^2)        FP32 opening prefilter
+  float4 L;   // (cx_lo, cy_lo, cz_lo, next as bits)   FP32 residuals + skip index
+  float4 Mh;  // (comx_hi, comy_hi, comz_hi, mass)     mixed-precision interaction
+  float4 Ml;  // (comx_lo, comy_lo, comz_lo, 0)
+};
+
 struct NodeArrays {
-  float4* A;     // (cx_hi, cy_hi, cz_hi, size^2)        FP32 opening prefilter
-  float4* L;     // (cx_lo, cy_lo, cz_lo, next as bits)   FP32 residuals + skip index
+  WalkRec* R;    // walk records (A, L, Mh, Ml)
   dvec4* C;      // (cx, cy, cz, size)                    exact opening test
   dvec4* M;      // (comx, comy, comz, mass)              interaction
   dvec4* F;      // (first moment x, y, z, mass)          build only
-  float4* Mh;    // (comx_hi, comy_hi, comz_hi, mass)     mixed-precision interaction
-  float4* Ml;    // (comx_lo, comy_lo, comz_lo, 0)
   int* first;    // first particle (sorted position)
   int* level;
 };
@@ -261,8 +266,8 @@ __global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64
       Lo.y = f32_lo(c[1], A.y);
       Lo.z = f32_lo(c[2], A.z);
       Lo.w = __int_as_float(next);
-      na.A[k] = A;
-      na.L[k] = Lo;
+      na.R[k].A = A;
+      na.R[k].L = Lo;
       na.C[k] = make_dvec4(c[0], c[1], c[2], size);
       na.first[k] = (int)i;
       na.level[k] = L;
@@ -322,20 +327,20 @@ __global__ void level_scatter_kernel(const int* __restrict__ level, int nnodes, 
   if (l >= 0) bucket[base + rank] = k;
 }
 
-__device__ __forceinline__ int node_next(const float4* __restrict__ L, int k) { return __float_as_int(L[k].w); }
+__device__ __forceinline__ int node_next(const WalkRec* __restrict__ R, int k) { return __float_as_int(R[k].L.w); }
 
 // FP32 hi/lo split of a cell's centre of mass, for the mixed-precision walk.
 __device__ __forceinline__ void store_mixed_com(const NodeArrays& na, int k, double x, double y, double z,
                                                 double m) {
   const float hx = (float)x, hy = (float)y, hz = (float)z;
-  na.Mh[k] = make_float4(hx, hy, hz, (float)m);
-  na.Ml[k] = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), 0.f);
+  na.R[k].Mh = make_float4(hx, hy, hz, (float)m);
+  na.R[k].Ml = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), 0.f);
 }
 
 __global__ void com_leaf_kernel(NodeArrays na, int nnodes, const uint32_t* __restrict__ perm,
                                 const double* __restrict__ pos, const double* __restrict__ mass) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nnodes || node_next(na.L, k) != k + 1) return;
+  if (k >= nnodes || node_next(na.R, k) != k + 1) return;
   const int64_t p = perm[na.first[k]];
   const double m = mass[p];
   const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
@@ -349,10 +354,10 @@ __global__ void com_level_kernel(NodeArrays na, const int* __restrict__ bucket, 
   const int b0 = off[level], b1 = off[level + 1];
   for (int t = b0 + blockIdx.x * blockDim.x + threadIdx.x; t < b1; t += gridDim.x * blockDim.x) {
     const int k = bucket[t];
-    const int nx = node_next(na.L, k);
+    const int nx = node_next(na.R, k);
     if (nx == k + 1) continue;  // leaf
     double fx = 0.0, fy = 0.0, fz = 0.0, m = 0.0;
-    for (int c = k + 1; c < nx; c = node_next(na.L, c)) {
+    for (int c = k + 1; c < nx; c = node_next(na.R, c)) {
       const dvec4 f = na.F[c];
       fx = dadd(fx, f.x);
       fy = dadd(fy, f.y);
@@ -391,8 +396,7 @@ constexpr int TW_FOLD = 32;
 
 template <bool GUARD, bool MIXED, class Epi>
 __global__ void __launch_bounds__(TW_THREADS)
-    tree_walk_kernel(const float4* __restrict__ nA, const float4* __restrict__ nL, const dvec4* __restrict__ nC,
-                     const dvec4* __restrict__ nM, const float4* __restrict__ nMh, const float4* __restrict__ nMl,
+    tree_walk_kernel(const WalkRec* __restrict__ nR, const dvec4* __restrict__ nC, const dvec4* __restrict__ nM,
                      int nnodes, const double* __restrict__ tpos, const uint32_t* __restrict__ order, int64_t nt,
                      double eps2, double theta, float th2_lo, float th2_hi, Epi epi) {
   const int64_t slot = (int64_t)blockIdx.x * TW_THREADS + threadIdx.x;
@@ -415,11 +419,16 @@ __global__ void __launch_bounds__(TW_THREADS)
   int pending = 0;
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
+  WalkRec cur;
+  if (node < nnodes) cur = nR[node];
   while (node < nnodes) {
+    // The next cell in preorder is the usual successor (a lane opened this one):
+    // fetch it while this one is decided.
+    const WalkRec ahead = nR[node + 1 < nnodes ? node + 1 : node];
     int lane_next = skip;
     if (node >= skip) {
-      const float4 A = nA[node];
-      const float4 Lo = nL[node];
+      const float4 A = cur.A;
+      const float4 Lo = cur.L;
       const int nx = __float_as_int(Lo.w);
       bool accept = (nx == node + 1);  // leaf
       if (!accept) {
@@ -445,8 +454,8 @@ __global__ void __launch_bounds__(TW_THREADS)
       }
       if (accept) {
         if (MIXED) {
-          const float4 H = nMh[node];
-          const float4 Q = nMl[node];
+          const float4 H = cur.Mh;
+          const float4 Q = cur.Ml;
           const float dx = (H.x - h0) + (Q.x - l0);
           const float dy = (H.y - h1) + (Q.y - l1);
           const float dz = (H.z - h2) + (Q.z - l2);
@@ -489,7 +498,12 @@ __global__ void __launch_bounds__(TW_THREADS)
         lane_next = node + 1;
       }
     }
-    node = __reduce_min_sync(0xffffffffu, lane_next);
+    const int next_node = __reduce_min_sync(0xffffffffu, lane_next);
+    if (next_node == node + 1)
+      cur = ahead;
+    else if (next_node < nnodes)
+      cur = nR[next_node];
+    node = next_node;
   }
   if (MIXED) {
     ax = (double)hx + (double)qx + (double)px;
@@ -504,7 +518,7 @@ __global__ void __launch_bounds__(TW_THREADS)
 // ---------------------------------------------------------------------------
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
-  Buffer nA, nL, nC, nM, nF, nMh, nMl, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
+  Buffer nA, nC, nM, nF, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
   int* host_flags = nullptr;  // pinned: tie, maxdepth, nnodes
   int words = TREE_MIN_WORDS;
 };
@@ -513,13 +527,10 @@ static std::recursive_mutex g_tree_mu;
 
 static NodeArrays node_arrays(TreeWS& ws) {
   NodeArrays na;
-  na.A = (float4*)ws.nA.ptr;
-  na.L = (float4*)ws.nL.ptr;
+  na.R = (WalkRec*)ws.nA.ptr;
   na.C = (dvec4*)ws.nC.ptr;
   na.M = (dvec4*)ws.nM.ptr;
   na.F = (dvec4*)ws.nF.ptr;
-  na.Mh = (float4*)ws.nMh.ptr;
-  na.Ml = (float4*)ws.nMl.ptr;
   na.first = (int*)ws.first.ptr;
   na.level = (int*)ws.level.ptr;
   return na;
@@ -588,13 +599,10 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   const int maxdepth = ws.host_flags[1];
   const int nnodes = ws.host_flags[2];
   // 4. nodes
-  GH_TRY(ensure(ws.nA, (size_t)nnodes * sizeof(float4)));
-  GH_TRY(ensure(ws.nL, (size_t)nnodes * sizeof(float4)));
+  GH_TRY(ensure(ws.nA, (size_t)nnodes * sizeof(WalkRec)));
   GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nM, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nF, (size_t)nnodes * sizeof(dvec4)));
-  GH_TRY(ensure(ws.nMh, (size_t)nnodes * sizeof(float4)));
-  GH_TRY(ensure(ws.nMl, (size_t)nnodes * sizeof(float4)));
   GH_TRY(ensure(ws.first, (size_t)nnodes * sizeof(int)));
   GH_TRY(ensure(ws.level, (size_t)nnodes * sizeof(int)));
   NodeArrays na = node_arrays(ws);
@@ -631,8 +639,8 @@ template <bool G, bool MX, class Epi>
 static void launch_walk(const NodeArrays& na, const BuiltTree& bt, const double* tpos, const uint32_t* order,
                         int64_t nt, double eps2, double theta, float lo, float hi, const Epi& epi, cudaStream_t st) {
   const unsigned blocks = (unsigned)((nt + TW_THREADS - 1) / TW_THREADS);
-  tree_walk_kernel<G, MX, Epi><<<blocks, TW_THREADS, 0, st>>>(na.A, na.L, na.C, na.M, na.Mh, na.Ml, bt.nnodes, tpos,
-                                                              order, nt, eps2, theta, lo, hi, epi);
+  tree_walk_kernel<G, MX, Epi><<<blocks, TW_THREADS, 0, st>>>(na.R, na.C, na.M, bt.nnodes, tpos, order, nt, eps2,
+                                                              theta, lo, hi, epi);
 }
 
 template <class Epi>
