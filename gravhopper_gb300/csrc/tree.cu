@@ -419,16 +419,11 @@ __global__ void __launch_bounds__(TW_THREADS)
   int pending = 0;
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
-  WalkRec cur;
-  if (node < nnodes) cur = nR[node];
   while (node < nnodes) {
-    // The next cell in preorder is the usual successor (a lane opened this one):
-    // fetch it while this one is decided.
-    const WalkRec ahead = nR[node + 1 < nnodes ? node + 1 : node];
     int lane_next = skip;
     if (node >= skip) {
-      const float4 A = cur.A;
-      const float4 Lo = cur.L;
+      const float4 A = nR[node].A;
+      const float4 Lo = nR[node].L;
       const int nx = __float_as_int(Lo.w);
       bool accept = (nx == node + 1);  // leaf
       if (!accept) {
@@ -454,8 +449,8 @@ __global__ void __launch_bounds__(TW_THREADS)
       }
       if (accept) {
         if (MIXED) {
-          const float4 H = cur.Mh;
-          const float4 Q = cur.Ml;
+          const float4 H = nR[node].Mh;
+          const float4 Q = nR[node].Ml;
           const float dx = (H.x - h0) + (Q.x - l0);
           const float dy = (H.y - h1) + (Q.y - l1);
           const float dz = (H.z - h2) + (Q.z - l2);
@@ -498,12 +493,7 @@ __global__ void __launch_bounds__(TW_THREADS)
         lane_next = node + 1;
       }
     }
-    const int next_node = __reduce_min_sync(0xffffffffu, lane_next);
-    if (next_node == node + 1)
-      cur = ahead;
-    else if (next_node < nnodes)
-      cur = nR[next_node];
-    node = next_node;
+    node = __reduce_min_sync(0xffffffffu, lane_next);
   }
   if (MIXED) {
     ax = (double)hx + (double)qx + (double)px;
