@@ -249,7 +249,7 @@ def main():
                 "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
 
     secondary = {}
-    if not args.no_secondary:
+    if not args.no_secondary and rank == 0:
         secondary = measure_secondary(ic, dev, fp64_peak, achieved if args.precision == "mixed" else None)
 
     if rank == 0:

@@ -279,8 +279,8 @@ __device__ __forceinline__ void mixed_chunk(const float4* __restrict__ tile, con
   }
 }
 
-// The same chunk with scalar FP32 instructions (one target per instruction), for
-// comparison with the packed form on the same data layout.
+// The same chunk with scalar FP32 instructions (one target per instruction); its
+// sources are stored once each, (x, y, z, m), not duplicated per lane pair.
 template <bool GUARD, int P, int JT>
 __device__ __forceinline__ void mixed_chunk_scalar(const float4* __restrict__ tile, const f2* tx, const f2* ty,
                                                    const f2* tz, f2 E2, f2* hx, f2* hy, f2* hz, f2* lx, f2* ly,
@@ -299,15 +299,14 @@ __device__ __forceinline__ void mixed_chunk_scalar(const float4* __restrict__ ti
   for (int r = 0; r < R; r++) ax[r] = ay[r] = az[r] = 0.f;
 #pragma unroll 4
   for (int k = 0; k < JT; k++) {
-    const float4 a = tile[2 * k + 0];
-    const float4 b = tile[2 * k + 1];
+    const float4 a = tile[k];  // (x, y, z, m): the scalar loop's undoubled layout
 #pragma unroll
     for (int r = 0; r < R; r++) {
-      const float dx = a.x - sx[r], dy = a.z - sy[r], dz = b.x - sz[r];
+      const float dx = a.x - sx[r], dy = a.y - sy[r], dz = a.z - sz[r];
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, e2)));
       float ri = rsqrt_approx(r2);
       if (GUARD) ri = r2 > 0.f ? ri : 0.f;
-      const float sc = (b.z * ri) * (ri * ri);
+      const float sc = (a.w * ri) * (ri * ri);
       ax[r] = fmaf(sc, dx, ax[r]);
       ay[r] = fmaf(sc, dy, ay[r]);
       az[r] = fmaf(sc, dz, az[r]);
@@ -386,8 +385,12 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
     for (int64_t c = c0; c < c1; c++) {
       float4* tb = tile + buf * (2 * JT);
-      tb[2 * tid + 0] = make_float4(pre.x, pre.x, pre.y, pre.y);
-      tb[2 * tid + 1] = make_float4(pre.z, pre.z, pre.w, pre.w);
+      if (PACKED) {
+        tb[2 * tid + 0] = make_float4(pre.x, pre.x, pre.y, pre.y);
+        tb[2 * tid + 1] = make_float4(pre.z, pre.z, pre.w, pre.w);
+      } else {
+        tb[tid] = pre;
+      }
       __syncthreads();
       if (c + 1 < c1) {
         const int64_t j = (c + 1) * JT + tid;
