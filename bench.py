@@ -366,19 +366,15 @@ def measure_tree(dev, n=1 << 20, steps=2):
                               "walk_ms_per_step": walk_ms / max(walks, 1),
                               "build_ms_per_step": t / steps * 1e3 - walk_ms / max(walks, 1)}
     # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
-    # full serial build plus the walk of 2048 targets, scaled to all N targets.
+    # its serial build plus the threaded walk of 2048 targets scaled to all N targets.
     rng = np.random.default_rng(0)
     idx = rng.choice(n, size=2048, replace=False)
     for theta in (0.7, 0.5):
-        t0 = time.perf_counter()
-        oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx[:1]], 0.1, theta, nthreads=1)
-        t_build = time.perf_counter() - t0
-        t0 = time.perf_counter()
+        tt = [0.0, 0.0]
         oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx], 0.1, theta,
-                                   nthreads=oracle.default_threads())
-        t_all = time.perf_counter() - t0
-        walk = max(t_all - t_build, 0.0) * n / idx.size
-        out[f"theta_{theta}"]["cpu_reference_s_per_step"] = t_build + walk
+                                   nthreads=oracle.default_threads(), times=tt)
+        out[f"theta_{theta}"]["cpu_reference_s_per_step"] = tt[0] + tt[1] * n / idx.size
+        out[f"theta_{theta}"]["cpu_reference_build_s"] = tt[0]
         out[f"theta_{theta}"]["cpu_reference_cores"] = oracle.default_threads()
     return out
 

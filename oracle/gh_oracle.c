@@ -25,6 +25,7 @@
  */
 #include <math.h>
 #include <pthread.h>
+#include <time.h>
 #include <stdint.h>
 #include <stdlib.h>
 #include <string.h>
@@ -339,10 +340,19 @@ int ghor_direct(const double *pos, const double *mass, int64_t np, const double 
  * pos (tree_force) or hold separate points (tree_force_position).  np == 0 gives
  * zeros (the reference reads pos[0] out of bounds there).
  */
+static double now_s(void)
+{
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+/* times_out (optional, 2 doubles): seconds spent building the tree and walking it. */
 int ghor_tree(const double *pos, const double *mass, int64_t np, const double *tpos,
               int64_t nt, double eps, double theta, double *out, int nthreads,
-              int maxdepth, int64_t *nnodes_out)
+              int maxdepth, int64_t *nnodes_out, double *times_out)
 {
+    double t0 = now_s();
     if (np < 0 || nt < 0) return GHOR_ERR_ARG;
     if (np == 0) {
         memset(out, 0, sizeof(double) * 3 * (size_t)nt);
@@ -364,6 +374,7 @@ int ghor_tree(const double *pos, const double *mass, int64_t np, const double *t
         }
     }
     ortree_finalize(&t);
+    double t1 = now_s();
     if (nnodes_out) *nnodes_out = t.count;
     job j;
     memset(&j, 0, sizeof(j));
@@ -375,6 +386,10 @@ int ghor_tree(const double *pos, const double *mass, int64_t np, const double *t
     j.theta = theta;
     j.out = out;
     run_threads(&j, nthreads);
+    if (times_out) {
+        times_out[0] = t1 - t0;
+        times_out[1] = now_s() - t1;
+    }
     free(t.nodes);
     return GHOR_OK;
 }

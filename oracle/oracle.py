@@ -61,7 +61,7 @@ def _load():
         lib.ghor_direct.restype = ctypes.c_int
         lib.ghor_tree.argtypes = [dp, dp, ctypes.c_int64, dp, ctypes.c_int64, ctypes.c_double,
                                   ctypes.c_double, dp, ctypes.c_int, ctypes.c_int,
-                                  ctypes.POINTER(ctypes.c_int64)]
+                                  ctypes.POINTER(ctypes.c_int64), dp]
         lib.ghor_tree.restype = ctypes.c_int
         lib.ghor_potential.argtypes = [dp, dp, ctypes.c_int64, ctypes.c_double, dp]
         lib.ghor_potential.restype = ctypes.c_int
@@ -107,16 +107,21 @@ def direct_summation_position(pos, mass, force_pos, eps, nthreads=None):
 
 
 def tree_force_position(pos, mass, force_pos, eps, theta=0.7, nthreads=None, maxdepth=4096,
-                        return_nodes=False):
-    """Oracle for ``_jbgrav.tree_force_position`` (gravhopper/_jbgrav.c:634-806)."""
+                        return_nodes=False, times=None):
+    """Oracle for ``_jbgrav.tree_force_position`` (gravhopper/_jbgrav.c:634-806).
+
+    ``times``: optional list that receives [build seconds, walk seconds]."""
     pos = _as_f64(pos)
     mass = _as_f64(mass)
     fp = _as_f64(force_pos)
     out = np.empty((fp.shape[0], 3))
     nn = ctypes.c_int64(0)
+    tt = np.zeros(2)
     rc = _load().ghor_tree(_dptr(pos), _dptr(mass), pos.shape[0], _dptr(fp), fp.shape[0],
                            float(eps), float(theta), _dptr(out), nthreads or default_threads(),
-                           int(maxdepth), ctypes.byref(nn))
+                           int(maxdepth), ctypes.byref(nn), _dptr(tt))
+    if times is not None:
+        times[:] = [float(tt[0]), float(tt[1])]
     if rc == 3:
         raise RuntimeError("oracle tree: depth limit exceeded (coincident particles?)")
     if rc:
