@@ -51,6 +51,8 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--cpu-targets", type=int, default=4096,
                     help="targets in the CPU-baseline sample (each against all N sources)")
+    ap.add_argument("--report", choices=["config0", "config1", "config4"],
+                    help="print one JSON line of the full measurements for that workload instead")
     return ap.parse_args()
 
 
@@ -163,6 +165,13 @@ def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.report:
+        import torch
+        dev = torch.device("cuda", 0)
+        torch.cuda.set_device(0)
+        fn = {"config0": report_config0, "config1": report_config1, "config4": report_config4}[args.report]
+        print(json.dumps({"report": args.report, **fn(dev)}), flush=True)
         return
     import numpy as np
     import torch
@@ -430,6 +439,113 @@ def measure_adjoint(dev, n=16384, steps=200):
         out[f"checkpoint_{k}"] = {"forward_ms": (t1 - t0) * 1e3, "backward_ms": (t2 - t1) * 1e3,
                                   "backward_over_forward": (t2 - t1) / (t1 - t0)}
     return out
+
+
+def report_config0(dev):
+    """The reference's own example: Plummer N=2000, 400 DKD steps through Simulation.run."""
+    import numpy as np
+
+    import gravhopper_gb300 as gh
+    from gravhopper_gb300 import ics
+    from oracle import oracle
+    ic = ics.plummer(2000, b=1e-3, totmass=1e6, seed=0)
+    out = {"n": 2000, "steps": 400}
+    e0 = oracle.total_energy(ic["pos"], ic["vel"], ic["mass"], 5e-5)
+    for prec in ("fp64", "mixed"):
+        sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct", precision=prec)
+        sim.add_IC(ic)
+        sim.run(2)
+        sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct", precision=prec)
+        sim.add_IC(ic)
+        t = _timed(lambda: sim.run(400))
+        e1 = oracle.total_energy(sim.positions[400], sim.velocities[400], ic["mass"], 5e-5)
+        out[prec] = {"run_s": t, "steps_per_s": 400 / t, "energy_drift": (e1 - e0) / abs(e0)}
+    t0 = time.perf_counter()
+    rx, rv = oracle.dkd_run(ic["pos"], ic["vel"], ic["mass"], 0.005, 5e-5, 400)
+    out["cpu_oracle_run_s"] = time.perf_counter() - t0
+    out["cpu_oracle_cores"] = oracle.default_threads()
+    sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct", precision="fp64")
+    sim.add_IC(ic)
+    sim.run(400)
+    out["fp64_final_state_equals_oracle"] = bool(np.array_equal(sim.positions[400], rx) and
+                                                 np.array_equal(sim.velocities[400], rv))
+    return out
+
+
+def report_config1(dev):
+    """Plummer N = 65,536 / 262,144 / 1,048,576, 10 DKD steps, FP64 and mixed: Gpair/s,
+    relative acceleration error (4096 sampled targets against the FP64 form, which is
+    bit-identical to the reference) and energy drift (FP64 energies)."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    out = {}
+    for n in (65536, 262144, 1 << 20):
+        ic = ics.plummer(n, seed=11)
+        m = torch.from_numpy(ic["mass"]).to(dev)
+        x0 = torch.from_numpy(ic["pos"]).to(dev)
+        v0 = torch.from_numpy(ic["vel"]).to(dev)
+        rng = np.random.default_rng(3)
+        idx = torch.from_numpy(rng.choice(n, size=4096, replace=False)).to(dev)
+        a64 = engine.direct_force(x0, m, 5e-5, force_pos=x0[idx].contiguous(), precision="fp64")
+        am = engine.direct_force(x0, m, 5e-5, precision="mixed")[idx]
+        err = torch.linalg.norm(am - a64, dim=1) / torch.linalg.norm(a64, dim=1)
+        e0 = engine.energy(x0, v0, m, 5e-5)[2]
+        row = {"rel_err_rms": float(torch.sqrt(torch.mean(err * err))), "rel_err_max": float(err.max())}
+        pairs = float(n) * (n - 1)
+        for prec in ("mixed", "fp64"):
+            steps = 10 if (prec == "mixed" or n <= 262144) else 1
+            x, v = x0.clone(), v0.clone()
+            t = _timed(lambda: engine.run_dkd(x, v, m, steps, 0.005, 5e-5, precision=prec))
+            r = {"steps": steps, "ms_per_step": t / steps * 1e3, "gpair_s": pairs * steps / t / 1e9}
+            if steps == 10:
+                r["energy_drift_10_steps"] = abs(engine.energy(x, v, m, 5e-5)[2] - e0) / abs(e0)
+            row[prec] = r
+        row["mixed_over_fp64"] = row["mixed"]["gpair_s"] / row["fp64"]["gpair_s"]
+        out[f"n_{n}"] = row
+    return out
+
+
+def report_config4(dev, n=16384, steps=20, ncoord=64):
+    """Adjoint gradients against FP64 central finite differences on 64 random
+    coordinates (FP64 rollout of `steps` steps at N = 16,384)."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    from gravhopper_gb300.adjoint import rollout
+    ic = ics.plummer(n, seed=0)
+    rng = np.random.default_rng(1)
+    x0 = torch.from_numpy(ic["pos"]).to(dev)
+    v0 = torch.from_numpy(ic["vel"]).to(dev)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
+    vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()
+    engine.run_dkd(xt, vt, m, steps, 0.005, 5e-5, precision="fp64")
+    xa = x0.clone().requires_grad_(True)
+    xT, _ = rollout(xa, v0, m, steps, 0.005, 5e-5, checkpoint_every=5, precision="fp64")
+    ((xT - xt) ** 2).mean().backward()
+    g = xa.grad.reshape(-1).cpu().numpy()
+
+    def loss_at(xp):
+        x, v = xp.reshape(-1, 3).clone(), v0.clone()
+        engine.run_dkd(x, v, m, steps, 0.005, 5e-5, precision="fp64")
+        return float(((x - xt) ** 2).mean())
+
+    idx = rng.choice(3 * n, size=ncoord, replace=False)
+    h = 1e-9
+    flat = x0.reshape(-1)
+    fd = []
+    for i in idx:
+        xp, xm = flat.clone(), flat.clone()
+        xp[i] += h
+        xm[i] -= h
+        fd.append((loss_at(xp) - loss_at(xm)) / (2 * h))
+    fd = np.array(fd)
+    rel = np.abs(fd - g[idx]) / np.maximum(np.abs(g[idx]), 1e-3 * np.abs(g).max())
+    return {"n": n, "steps": steps, "coordinates": ncoord, "fd_step_kpc": h,
+            "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel))}
 
 
 if __name__ == "__main__":
