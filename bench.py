@@ -458,7 +458,7 @@ def report_config0(dev):
         sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct", precision=prec)
         sim.add_IC(ic)
         t = _timed(lambda: sim.run(400))
-        e1 = oracle.total_energy(sim.positions[400], sim.velocities[400], ic["mass"], 5e-5)
+        e1 = oracle.total_energy(sim._pos[400], sim._vel[400], ic["mass"], 5e-5)
         out[prec] = {"run_s": t, "steps_per_s": 400 / t, "energy_drift": (e1 - e0) / abs(e0)}
     t0 = time.perf_counter()
     rx, rv = oracle.dkd_run(ic["pos"], ic["vel"], ic["mass"], 0.005, 5e-5, 400)
@@ -467,8 +467,8 @@ def report_config0(dev):
     sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct", precision="fp64")
     sim.add_IC(ic)
     sim.run(400)
-    out["fp64_final_state_equals_oracle"] = bool(np.array_equal(sim.positions[400], rx) and
-                                                 np.array_equal(sim.velocities[400], rv))
+    out["fp64_final_state_equals_oracle"] = bool(np.array_equal(sim._pos[400], rx) and
+                                                 np.array_equal(sim._vel[400], rv))
     return out
 
 
@@ -507,45 +507,50 @@ def report_config1(dev):
     return out
 
 
-def report_config4(dev, n=16384, steps=20, ncoord=64):
-    """Adjoint gradients against FP64 central finite differences on 64 random
-    coordinates (FP64 rollout of `steps` steps at N = 16,384)."""
+def report_config4(dev, n=16384):
+    """Adjoint gradients with respect to x0 against FP64 central finite differences
+    (FP64 rollouts, N = 16,384): 64 random coordinates over 20 steps, and 8 over the
+    full 200-step rollout with checkpoints every 20 steps."""
     import numpy as np
     import torch
 
     from gravhopper_gb300 import engine, ics
     from gravhopper_gb300.adjoint import rollout
     ic = ics.plummer(n, seed=0)
-    rng = np.random.default_rng(1)
     x0 = torch.from_numpy(ic["pos"]).to(dev)
     v0 = torch.from_numpy(ic["vel"]).to(dev)
     m = torch.from_numpy(ic["mass"]).to(dev)
-    xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
-    vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()
-    engine.run_dkd(xt, vt, m, steps, 0.005, 5e-5, precision="fp64")
-    xa = x0.clone().requires_grad_(True)
-    xT, _ = rollout(xa, v0, m, steps, 0.005, 5e-5, checkpoint_every=5, precision="fp64")
-    ((xT - xt) ** 2).mean().backward()
-    g = xa.grad.reshape(-1).cpu().numpy()
+    out = {"n": n}
+    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (200, 8, 20, (1e-9, 1e-11))):
+        rng = np.random.default_rng(1)
+        xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
+        vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()
+        engine.run_dkd(xt, vt, m, steps, 0.005, 5e-5, precision="fp64")
+        xa = x0.clone().requires_grad_(True)
+        xT, _ = rollout(xa, v0, m, steps, 0.005, 5e-5, checkpoint_every=ckpt, precision="fp64")
+        ((xT - xt) ** 2).mean().backward()
+        g = xa.grad.reshape(-1).cpu().numpy()
 
-    def loss_at(xp):
-        x, v = xp.reshape(-1, 3).clone(), v0.clone()
-        engine.run_dkd(x, v, m, steps, 0.005, 5e-5, precision="fp64")
-        return float(((x - xt) ** 2).mean())
+        def loss_at(xp):
+            x, v = xp.reshape(-1, 3).clone(), v0.clone()
+            engine.run_dkd(x, v, m, steps, 0.005, 5e-5, precision="fp64")
+            return float(((x - xt) ** 2).mean())
 
-    idx = rng.choice(3 * n, size=ncoord, replace=False)
-    h = 1e-9
-    flat = x0.reshape(-1)
-    fd = []
-    for i in idx:
-        xp, xm = flat.clone(), flat.clone()
-        xp[i] += h
-        xm[i] -= h
-        fd.append((loss_at(xp) - loss_at(xm)) / (2 * h))
-    fd = np.array(fd)
-    rel = np.abs(fd - g[idx]) / np.maximum(np.abs(g[idx]), 1e-3 * np.abs(g).max())
-    return {"n": n, "steps": steps, "coordinates": ncoord, "fd_step_kpc": h,
-            "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel))}
+        idx = rng.choice(3 * n, size=ncoord, replace=False)
+        flat = x0.reshape(-1)
+        row = {"coordinates": ncoord, "checkpoint_every": ckpt}
+        for h in hs:
+            fd = []
+            for i in idx:
+                xp, xm = flat.clone(), flat.clone()
+                xp[i] += h
+                xm[i] -= h
+                fd.append((loss_at(xp) - loss_at(xm)) / (2 * h))
+            fd = np.array(fd)
+            rel = np.abs(fd - g[idx]) / np.maximum(np.abs(g[idx]), 1e-3 * np.abs(g).max())
+            row[f"h_{h:g}"] = {"rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel))}
+        out[f"steps_{steps}"] = row
+    return out
 
 
 if __name__ == "__main__":
