@@ -357,7 +357,9 @@ def measure_tree(dev, n=1 << 20, steps=2):
     from oracle import oracle
     ic = ics.hernquist_disk(n, seed=1)
     m = torch.from_numpy(ic["mass"]).to(dev)
-    out = {"n": n, "workload": "Hernquist (70%) + exponential disk (30%), 1e11 Msun, eps=0.1 kpc, dt=0.5 Myr"}
+    l2 = _capi.measure_l2_read()
+    out = {"n": n, "workload": "Hernquist (70%) + exponential disk (30%), 1e11 Msun, eps=0.1 kpc, dt=0.5 Myr",
+           "l2_read_gbs_measured": l2 / 1e9}
     for theta in (0.7, 0.5):
         key = f"theta_{theta}"
         out[key] = {}
@@ -371,9 +373,25 @@ def measure_tree(dev, n=1 << 20, steps=2):
                                               precision=prec))
             _capi.kernel_timing(False)
             walk_ms, walks = _capi.kernel_timing_collect()
+            walk_s = walk_ms / max(walks, 1) * 1e-3
+            # one more step with the walk counters on (not timed)
+            _capi.tree_stats_read()
+            _capi.tree_stats(True)
+            engine.run_dkd(x, v, m, 1, 0.5, 0.1, algorithm="tree", theta=theta, precision=prec)
+            _capi.tree_stats(False)
+            c = _capi.tree_stats_read()
+            rec_bytes = 64 * c["cell_steps"]
             out[key][prec] = {"particle_steps_per_s": n * steps / t, "ms_per_step": t / steps * 1e3,
-                              "walk_ms_per_step": walk_ms / max(walks, 1),
-                              "build_ms_per_step": t / steps * 1e3 - walk_ms / max(walks, 1)}
+                              "walk_ms_per_step": walk_s * 1e3,
+                              "build_ms_per_step": t / steps * 1e3 - walk_s * 1e3,
+                              "interactions_per_target": c["interactions"] / n,
+                              "cells_visited_per_target": c["target_visits"] / n,
+                              "exact_tests_per_target": c["exact_tests"] / n,
+                              "warp_cell_steps": c["cell_steps"],
+                              "record_bytes_per_walk": rec_bytes,
+                              "record_read_gbs": rec_bytes / walk_s / 1e9,
+                              "record_read_frac_of_measured_l2": rec_bytes / walk_s / l2,
+                              "per_target_record_gbs": 64 * c["target_visits"] / walk_s / 1e9}
     # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
     # its serial build plus the threaded walk of 2048 targets scaled to all N targets.
     rng = np.random.default_rng(0)

@@ -82,6 +82,9 @@ SIGNATURES = {
     "gh_direct_num_shapes": (_int, []),
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),
+    "gh_measure_l2_read": (_int, [_vp, _vp]),
+    "gh_tree_stats": (_int, [_int]),
+    "gh_tree_stats_read": (_int, [_vp]),
 }
 
 
@@ -157,3 +160,24 @@ def kernel_timing_collect():
     n = ctypes.c_int64(0)
     call("gh_kernel_timing_collect", ctypes.addressof(ms), ctypes.addressof(n))
     return ms.value, n.value
+
+
+def measure_l2_read(stream=None):
+    """L2 read bandwidth (bytes/s) measured on the current device."""
+    b = ctypes.c_double(0.0)
+    call("gh_measure_l2_read", ctypes.addressof(b), stream_handle(stream))
+    return b.value
+
+
+def tree_stats(enable: bool) -> None:
+    """Turns the tree-walk counters on or off."""
+    call("gh_tree_stats", 1 if enable else 0)
+
+
+def tree_stats_read():
+    """Counters since the last read: walks, warp cell steps (64-byte records read),
+    cells visited summed over targets, target-cell interactions, exact FP64 opening tests."""
+    out = (ctypes.c_int64 * 5)()
+    call("gh_tree_stats_read", ctypes.addressof(out))
+    return {"walks": out[0], "cell_steps": out[1], "target_visits": out[2], "interactions": out[3],
+            "exact_tests": out[4]}

@@ -398,7 +398,8 @@ template <bool GUARD, bool MIXED, class Epi>
 __global__ void __launch_bounds__(TW_THREADS)
     tree_walk_kernel(const WalkRec* __restrict__ nR, const dvec4* __restrict__ nC, const dvec4* __restrict__ nM,
                      int nnodes, const double* __restrict__ tpos, const uint32_t* __restrict__ order, int64_t nt,
-                     double eps2, double theta, float th2_lo, float th2_hi, Epi epi) {
+                     double eps2, double theta, float th2_lo, float th2_hi, Epi epi,
+                     unsigned long long* __restrict__ stats) {
   const int64_t slot = (int64_t)blockIdx.x * TW_THREADS + threadIdx.x;
   const bool valid = slot < nt;
   const int64_t t = valid ? (order ? (int64_t)order[slot] : slot) : 0;
@@ -417,11 +418,14 @@ __global__ void __launch_bounds__(TW_THREADS)
   float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
   float hx = 0.f, hy = 0.f, hz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;  // two-sum hi, lo
   int pending = 0;
+  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0;  // walk counters (read when stats != nullptr)
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
   while (node < nnodes) {
+    n_step++;
     int lane_next = skip;
     if (node >= skip) {
+      n_visit++;
       const float4 A = nR[node].A;
       const float4 Lo = nR[node].L;
       const int nx = __float_as_int(Lo.w);
@@ -439,6 +443,7 @@ __global__ void __launch_bounds__(TW_THREADS)
           accept = false;
         } else {
           // gravoct_calc_accel opening test with the reference's FP64 operations
+          n_exact++;
           const dvec4 C = nC[node];
           const double e0 = dsub(C.x, p0), e1 = dsub(C.y, p1), e2 = dsub(C.z, p2);
           double nd = dmul(e0, e0);
@@ -448,6 +453,7 @@ __global__ void __launch_bounds__(TW_THREADS)
         }
       }
       if (accept) {
+        n_inter++;
         if (MIXED) {
           const float4 H = nR[node].Mh;
           const float4 Q = nR[node].Ml;
@@ -494,6 +500,18 @@ __global__ void __launch_bounds__(TW_THREADS)
       }
     }
     node = __reduce_min_sync(0xffffffffu, lane_next);
+  }
+  if (stats) {
+    // one cell record read per warp step; the other counts summed over lanes
+    n_visit = __reduce_add_sync(0xffffffffu, n_visit);
+    n_inter = __reduce_add_sync(0xffffffffu, n_inter);
+    n_exact = __reduce_add_sync(0xffffffffu, n_exact);
+    if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&stats[0], (unsigned long long)n_step);
+      atomicAdd(&stats[1], (unsigned long long)n_visit);
+      atomicAdd(&stats[2], (unsigned long long)n_inter);
+      atomicAdd(&stats[3], (unsigned long long)n_exact);
+    }
   }
   if (MIXED) {
     ax = (double)hx + (double)qx + (double)px;
@@ -625,12 +643,20 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   return GH_OK;
 }
 
+// Walk counters, off unless gh_tree_stats(1): [0] warp cell steps (one 64-byte
+// record read each), [1] cells visited summed over targets, [2] target-cell
+// interactions, [3] exact FP64 opening tests.
+static bool g_stats_on = false;
+static int64_t g_stats_walks = 0;
+static Buffer g_stats[64];
+
 template <bool G, bool MX, class Epi>
 static void launch_walk(const NodeArrays& na, const BuiltTree& bt, const double* tpos, const uint32_t* order,
-                        int64_t nt, double eps2, double theta, float lo, float hi, const Epi& epi, cudaStream_t st) {
+                        int64_t nt, double eps2, double theta, float lo, float hi, const Epi& epi,
+                        unsigned long long* stats, cudaStream_t st) {
   const unsigned blocks = (unsigned)((nt + TW_THREADS - 1) / TW_THREADS);
   tree_walk_kernel<G, MX, Epi><<<blocks, TW_THREADS, 0, st>>>(na.R, na.C, na.M, bt.nnodes, tpos, order, nt, eps2,
-                                                              theta, lo, hi, epi);
+                                                              theta, lo, hi, epi, stats);
 }
 
 template <class Epi>
@@ -646,17 +672,29 @@ static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const 
   NodeArrays na = node_arrays(ws);
   const bool mixed = precision == GH_PREC_MIXED;
   const bool guard = mixed ? !((float)eps2 > 0.f) : eps2 == 0.0;
+  unsigned long long* stats = nullptr;
+  if (g_stats_on) {
+    DeviceInfo di;
+    GH_TRY(device_info(&di));
+    Buffer& b = g_stats[di.device];
+    if (!b.ptr) {
+      GH_TRY(ensure(b, 4 * sizeof(unsigned long long)));
+      GH_CUDA_TRY(cudaMemsetAsync(b.ptr, 0, 4 * sizeof(unsigned long long), st));
+    }
+    stats = (unsigned long long*)b.ptr;
+    g_stats_walks++;
+  }
   prof_begin(st);
   if (mixed) {
     if (guard)
-      launch_walk<true, true>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+      launch_walk<true, true>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, stats, st);
     else
-      launch_walk<false, true>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+      launch_walk<false, true>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, stats, st);
   } else {
     if (guard)
-      launch_walk<true, false>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+      launch_walk<true, false>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, stats, st);
     else
-      launch_walk<false, false>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, st);
+      launch_walk<false, false>(na, bt, tpos, order, nt, eps2, theta, lo, hi, epi, stats, st);
   }
   prof_end(st);
   GH_LAUNCH_CHECK();
@@ -727,3 +765,32 @@ int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nstep
 }
 
 }  // namespace gh
+
+extern "C" int gh_tree_stats(int enable) {
+  using namespace gh;
+  clear_error();
+  std::lock_guard<std::recursive_mutex> lk(g_tree_mu);
+  g_stats_on = enable != 0;
+  return GH_OK;
+}
+
+extern "C" int gh_tree_stats_read(int64_t* out) {
+  using namespace gh;
+  clear_error();
+  if (!out) return set_error(GH_ERR_ARG, "tree stats: null output");
+  std::lock_guard<std::recursive_mutex> lk(g_tree_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  Buffer& b = g_stats[di.device];
+  unsigned long long h[4] = {0, 0, 0, 0};
+  if (b.ptr) {
+    GH_CUDA_TRY(cudaDeviceSynchronize());
+    GH_CUDA_TRY(cudaMemcpy(h, b.ptr, sizeof(h), cudaMemcpyDeviceToHost));
+    GH_CUDA_TRY(cudaMemset(b.ptr, 0, sizeof(h)));
+    GH_CUDA_TRY(cudaDeviceSynchronize());
+  }
+  out[0] = g_stats_walks;
+  for (int k = 0; k < 4; k++) out[k + 1] = (int64_t)h[k];
+  g_stats_walks = 0;
+  return GH_OK;
+}

@@ -178,6 +178,23 @@ int gh_kernel_timing(int enable);
  * total milliseconds and number of timed launches; clears the record. */
 int gh_kernel_timing_collect(double* total_ms, int64_t* launches);
 
+/* Measures the current device's L2 read bandwidth (bytes/s) with 16-byte L1-bypassing
+ * loads over a 32 MiB buffer read 64 times (no counterpart in the reference).  The
+ * roofline denominator of the tree walk, whose cell records stay in L2. */
+int gh_measure_l2_read(double* bytes_per_s, void* stream);
+
+/* Enables (1) or disables (0) the tree-walk counters (no counterpart in the
+ * reference, which counts nothing).  While enabled every walk adds, over its warps,
+ * the cell steps (one 64-byte cell record read per warp step), the cells visited by
+ * each target (what a per-target walk would read), the target-cell interactions and
+ * the exact FP64 opening tests. */
+int gh_tree_stats(int enable);
+
+/* Synchronises the device and returns the counters accumulated since the last read,
+ * then clears them: out[0] walks, out[1] warp cell steps, out[2] target cell visits,
+ * out[3] interactions, out[4] exact opening tests. */
+int gh_tree_stats_read(int64_t* out);
+
 #ifdef __cplusplus
 }
 #endif

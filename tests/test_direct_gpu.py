@@ -106,3 +106,12 @@ def test_invalid_arguments_raise(lib, cuda):
     from gravhopper_gb300 import _capi, _jbgrav
     with pytest.raises(_capi.EngineError):
         _jbgrav.direct_summation(np.zeros((3, 3)), np.ones(3), -1.0)
+
+
+def test_throughput_probes(lib, cuda):
+    """The roofline denominators are measured, positive and of a plausible size."""
+    from gravhopper_gb300 import _capi
+    f32, f64 = _capi.measure_fma_peaks()
+    assert 1e12 < f32 < 1e15 and 1e10 < f64 < f32
+    l2 = _capi.measure_l2_read()
+    assert 1e12 < l2 < 1e15

@@ -148,3 +148,29 @@ def test_simulation_default_tree(golden, lib, cuda):
     sim.add_IC({"pos": golden["plummer_pos"], "vel": golden["plummer_vel"], "mass": golden["plummer_mass"]})
     sim.run(20)
     np.testing.assert_allclose(sim.positions[20], golden["traj_tree_x_20"], rtol=0, atol=1e-12)
+
+
+def test_tree_walk_counters(lib, cuda):
+    """theta = 0 opens every internal cell, so each target visits every cell once and
+    interacts with every leaf (one per particle); each warp steps through all cells."""
+    from gravhopper_gb300 import _capi, _jbgrav, ics
+    n = 5000
+    ic = ics.plummer(n, seed=8)
+    _capi.tree_stats_read()
+    _capi.tree_stats(True)
+    try:
+        _jbgrav.tree_force(ic["pos"], ic["mass"], 5e-5, 0.0)
+        c0 = _capi.tree_stats_read()
+        _jbgrav.tree_force(ic["pos"], ic["mass"], 5e-5, 0.7)
+        c7 = _capi.tree_stats_read()
+    finally:
+        _capi.tree_stats(False)
+    assert c0["walks"] == 1 and c0["interactions"] == n * n
+    assert c0["target_visits"] % n == 0
+    ncells = c0["target_visits"] // n
+    assert ncells > n
+    assert c0["cell_steps"] == (n + 31) // 32 * ncells
+    assert c7["walks"] == 1
+    assert 0 < c7["interactions"] < c7["target_visits"] < c0["target_visits"]
+    assert c7["cell_steps"] * 32 >= c7["target_visits"] and c7["exact_tests"] <= c7["target_visits"]
+    assert _capi.tree_stats_read()["walks"] == 0
