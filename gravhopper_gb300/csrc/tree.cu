@@ -10,7 +10,8 @@
 //      branch number, _jbgrav.c:441-450), so key order is depth-first order with
 //      children in branch order 0..7.  The number of words grows until no two
 //      particles share a full key (coincident particles end with GH_ERR_DEPTH);
-//   3. stable radix sort of the keys;
+//   3. sort of the keys: a radix sort of the first word, then runs of equal first
+//      words ordered by the other words (a full multi-word radix sort for long runs);
 //   4. the node set of the reference's uncompressed octree (every cell that holds a
 //      particle and whose parent holds at least two, single-child chains included)
 //      laid out in depth-first preorder with skip ("next") indices, from the common
@@ -176,6 +177,72 @@ __device__ __forceinline__ int key_lcp(const uint64_t* __restrict__ keys, int wo
 __device__ __forceinline__ unsigned key_digit(const uint64_t* __restrict__ keys, int64_t n, int64_t i, int level) {
   const int w = level / KEY_LEVELS, l = level - w * KEY_LEVELS;
   return (unsigned)((keys[(int64_t)w * n + i] >> (3 * (KEY_LEVELS - 1 - l))) & 7u);
+}
+
+// ---------------------------------------------------------------------------
+// 3. Sort: the first key word with a radix sort, then the rare runs of equal first
+//    words ordered by the remaining words in place.  Equal full keys make the build
+//    widen the keys and start again, so the final order is the full-key order.
+// ---------------------------------------------------------------------------
+constexpr int TIE_MAX_RUN = 256;  // longer runs of equal first words: full radix sort
+
+// Brings key words 1.. into the order of the sorted first word: out[w][i] = in[w][idx[i]].
+__global__ void gather_words_kernel(const uint64_t* __restrict__ kin, uint64_t* __restrict__ kout, int words,
+                                    int64_t n, const uint32_t* __restrict__ idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const int64_t src = idx[i];
+  for (int w = 1; w < words; w++) kout[(int64_t)w * n + i] = kin[(int64_t)w * n + src];
+}
+
+__device__ __forceinline__ bool tied_first_word(const uint64_t* __restrict__ k0, int64_t n, int64_t i) {
+  const uint64_t k = k0[i];
+  return (i > 0 && k0[i - 1] == k) || (i + 1 < n && k0[i + 1] == k);
+}
+
+// Each particle in a run of equal first words takes its rank within the run by
+// (words 1.., original index) and writes its key and index to that slot of the
+// temporaries; flags[2] marks a run longer than TIE_MAX_RUN.
+__global__ void tie_rank_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
+                                const uint32_t* __restrict__ idx, uint64_t* __restrict__ kt,
+                                uint32_t* __restrict__ it, int* __restrict__ flags) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !tied_first_word(keys, n, i)) return;
+  const uint64_t k = keys[i];
+  int64_t s = i, e = i + 1;
+  while (s > 0 && keys[s - 1] == k) {
+    if (i - --s >= TIE_MAX_RUN) {
+      atomicOr(&flags[2], 1);
+      return;
+    }
+  }
+  while (e < n && keys[e] == k) {
+    if (++e - i > TIE_MAX_RUN) {
+      atomicOr(&flags[2], 1);
+      return;
+    }
+  }
+  const uint32_t me = idx[i];
+  int64_t r = 0;
+  for (int64_t j = s; j < e; j++) {
+    if (j == i) continue;
+    int c = 0;  // -1: j before i, +1: j after i
+    for (int w = 1; w < words && c == 0; w++) {
+      const uint64_t a = keys[(int64_t)w * n + j], b = keys[(int64_t)w * n + i];
+      c = a < b ? -1 : (a > b ? 1 : 0);
+    }
+    if (c < 0 || (c == 0 && idx[j] < me)) r++;
+  }
+  for (int w = 1; w < words; w++) kt[(int64_t)w * n + s + r] = keys[(int64_t)w * n + i];
+  it[s + r] = me;
+}
+
+__global__ void tie_copy_kernel(uint64_t* __restrict__ keys, int words, int64_t n, uint32_t* __restrict__ idx,
+                                const uint64_t* __restrict__ kt, const uint32_t* __restrict__ it) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n || !tied_first_word(keys, n, i)) return;
+  for (int w = 1; w < words; w++) keys[(int64_t)w * n + i] = kt[(int64_t)w * n + i];
+  idx[i] = it[i];
 }
 
 // flags[0]: two particles share a full key; flags[1]: deepest leaf level.
@@ -527,7 +594,7 @@ __global__ void __launch_bounds__(TW_THREADS)
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
   Buffer nA, nC, nM, nF, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
-  int* host_flags = nullptr;  // pinned: tie, maxdepth, nnodes
+  int* host_flags = nullptr;  // pinned: tie, maxdepth, long run, nnodes
   int words = TREE_MIN_WORDS;
 };
 static TreeWS g_tree[64];
@@ -576,26 +643,45 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.idx_tmp, n * sizeof(uint32_t)));
   GH_TRY(ensure(ws.rs, radix_scratch_words(n) * sizeof(uint32_t)));
   // 2-3. keys, sort, prefix structure; widen the keys while particles tie
+  bool full_sort = false;
   for (;;) {
     const int words = ws.words;
     GH_TRY(ensure(ws.keys, (size_t)words * n * sizeof(uint64_t)));
     GH_TRY(ensure(ws.keys_tmp, (size_t)words * n * sizeof(uint64_t)));
     uint64_t* keys = (uint64_t*)ws.keys.ptr;
-    keys_kernel<<<gn, T, 0, st>>>(pos, n, root, words, keys, (uint32_t*)ws.idx.ptr);
+    uint64_t* ktmp = (uint64_t*)ws.keys_tmp.ptr;
+    uint32_t* idx = (uint32_t*)ws.idx.ptr;
+    uint32_t* itmp = (uint32_t*)ws.idx_tmp.ptr;
+    keys_kernel<<<gn, T, 0, st>>>(pos, n, root, words, keys, idx);
     GH_LAUNCH_CHECK();
-    GH_TRY(radix_sort_keys(keys, (uint32_t*)ws.idx.ptr, (uint64_t*)ws.keys_tmp.ptr, (uint32_t*)ws.idx_tmp.ptr,
-                           words, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
     GH_CUDA_TRY(cudaMemsetAsync(ws.flags.ptr, 0, 4 * sizeof(int), st));
+    if (full_sort) {
+      GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, words, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
+    } else {
+      GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, 1, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
+      gather_words_kernel<<<gn, T, 0, st>>>(keys, ktmp, words, n, idx);
+      GH_LAUNCH_CHECK();
+      GH_CUDA_TRY(cudaMemcpyAsync(keys + n, ktmp + n, (size_t)(words - 1) * n * sizeof(uint64_t),
+                                  cudaMemcpyDeviceToDevice, st));
+      tie_rank_kernel<<<gn, T, 0, st>>>(keys, words, n, idx, ktmp, itmp, (int*)ws.flags.ptr);
+      GH_LAUNCH_CHECK();
+      tie_copy_kernel<<<gn, T, 0, st>>>(keys, words, n, idx, ktmp, itmp);
+      GH_LAUNCH_CHECK();
+    }
     lcp_kernel<<<gn1, T, 0, st>>>(keys, words, n, (int*)ws.lp.ptr, (int*)ws.flags.ptr);
     GH_LAUNCH_CHECK();
     count_kernel<<<gn, T, 0, st>>>((const int*)ws.lp.ptr, n, (int*)ws.cnt.ptr, (int*)ws.depth.ptr,
                                    (int*)ws.flags.ptr);
     GH_LAUNCH_CHECK();
     GH_TRY(exclusive_scan_i32((const int*)ws.cnt.ptr, (int*)ws.base.ptr, n, (int*)ws.scan.ptr, st));
-    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 2, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 3, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
                                 st));
     GH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (ws.host_flags[2] && !full_sort) {  // a long run of equal first words
+      full_sort = true;
+      continue;
+    }
     if (!ws.host_flags[0]) break;
     if (ws.words >= TREE_MAX_WORDS)
       return set_error(GH_ERR_DEPTH,
@@ -605,7 +691,7 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   }
   const int words = ws.words;
   const int maxdepth = ws.host_flags[1];
-  const int nnodes = ws.host_flags[2];
+  const int nnodes = ws.host_flags[3];
   // 4. nodes
   GH_TRY(ensure(ws.nA, (size_t)nnodes * sizeof(WalkRec)));
   GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));

@@ -65,6 +65,21 @@ def test_tree_deep_levels_widen_keys(lib, cuda):
     check(_jbgrav.tree_force(pos, m, 1e-3, 0.6), oracle.tree_force(pos, m, 1e-3, 0.6))
 
 
+@pytest.mark.parametrize("clumps,per_clump", [(30, 100), (1, 2000)])
+def test_tree_dense_clumps(lib, cuda, clumps, per_clump):
+    """Clumps of side 1e-8 in a unit box share their first 21 levels: runs of up to
+    256 equal first key words are ordered in place, a longer run takes the full
+    multi-word sort."""
+    from gravhopper_gb300 import _jbgrav
+    rng = np.random.default_rng(6)
+    centres = rng.uniform(-1, 1, size=(clumps, 1, 3))
+    pos = (centres + 1e-8 * rng.uniform(0, 1, size=(clumps, per_clump, 3))).reshape(-1, 3)
+    pos = np.concatenate([pos, rng.uniform(-1, 1, size=(200, 3))])
+    m = rng.uniform(1, 2, size=len(pos))
+    for theta in (0.5, 0.7):
+        check(_jbgrav.tree_force(pos, m, 1e-10, theta), oracle.tree_force(pos, m, 1e-10, theta))
+
+
 def test_tree_coincident_particles_error(lib, cuda):
     from gravhopper_gb300 import _capi, _jbgrav
     pos = np.array([[0.0, 0.0, 0.0], [1.0, 2.0, 3.0], [1.0, 2.0, 3.0]])
