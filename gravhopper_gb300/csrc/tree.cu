@@ -461,7 +461,7 @@ __device__ __forceinline__ double rsqrt_f64(double s) {
 // The opening decisions are the same exact ones in both forms.
 constexpr int TW_FOLD = 32;
 
-template <bool GUARD, bool MIXED, class Epi>
+template <bool GUARD, bool MIXED, bool STATS, class Epi>
 __global__ void __launch_bounds__(TW_THREADS)
     tree_walk_kernel(const WalkRec* __restrict__ nR, const dvec4* __restrict__ nC, const dvec4* __restrict__ nM,
                      int nnodes, const double* __restrict__ tpos, const uint32_t* __restrict__ order, int64_t nt,
@@ -485,14 +485,14 @@ __global__ void __launch_bounds__(TW_THREADS)
   float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
   float hx = 0.f, hy = 0.f, hz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;  // two-sum hi, lo
   int pending = 0;
-  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0;  // walk counters (read when stats != nullptr)
+  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0;  // walk counters (STATS)
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
   while (node < nnodes) {
-    n_step++;
+    if (STATS) n_step++;
     int lane_next = skip;
     if (node >= skip) {
-      n_visit++;
+      if (STATS) n_visit++;
       const float4 A = nR[node].A;
       const float4 Lo = nR[node].L;
       const int nx = __float_as_int(Lo.w);
@@ -510,7 +510,7 @@ __global__ void __launch_bounds__(TW_THREADS)
           accept = false;
         } else {
           // gravoct_calc_accel opening test with the reference's FP64 operations
-          n_exact++;
+          if (STATS) n_exact++;
           const dvec4 C = nC[node];
           const double e0 = dsub(C.x, p0), e1 = dsub(C.y, p1), e2 = dsub(C.z, p2);
           double nd = dmul(e0, e0);
@@ -520,7 +520,7 @@ __global__ void __launch_bounds__(TW_THREADS)
         }
       }
       if (accept) {
-        n_inter++;
+        if (STATS) n_inter++;
         if (MIXED) {
           const float4 H = nR[node].Mh;
           const float4 Q = nR[node].Ml;
@@ -568,7 +568,7 @@ __global__ void __launch_bounds__(TW_THREADS)
     }
     node = __reduce_min_sync(0xffffffffu, lane_next);
   }
-  if (stats) {
+  if (STATS) {
     // one cell record read per warp step; the other counts summed over lanes
     n_visit = __reduce_add_sync(0xffffffffu, n_visit);
     n_inter = __reduce_add_sync(0xffffffffu, n_inter);
@@ -741,8 +741,12 @@ static void launch_walk(const NodeArrays& na, const BuiltTree& bt, const double*
                         int64_t nt, double eps2, double theta, float lo, float hi, const Epi& epi,
                         unsigned long long* stats, cudaStream_t st) {
   const unsigned blocks = (unsigned)((nt + TW_THREADS - 1) / TW_THREADS);
-  tree_walk_kernel<G, MX, Epi><<<blocks, TW_THREADS, 0, st>>>(na.R, na.C, na.M, bt.nnodes, tpos, order, nt, eps2,
-                                                              theta, lo, hi, epi, stats);
+  if (stats)
+    tree_walk_kernel<G, MX, true, Epi><<<blocks, TW_THREADS, 0, st>>>(na.R, na.C, na.M, bt.nnodes, tpos, order, nt,
+                                                                      eps2, theta, lo, hi, epi, stats);
+  else
+    tree_walk_kernel<G, MX, false, Epi><<<blocks, TW_THREADS, 0, st>>>(na.R, na.C, na.M, bt.nnodes, tpos, order,
+                                                                       nt, eps2, theta, lo, hi, epi, nullptr);
 }
 
 template <class Epi>
