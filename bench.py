@@ -393,15 +393,20 @@ def measure_tree(dev, n=1 << 20, steps=2):
                               "record_read_frac_of_measured_l2": rec_bytes / walk_s / l2,
                               "per_target_record_gbs": 64 * c["target_visits"] / walk_s / 1e9}
     # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
-    # its serial build plus the threaded walk of 2048 targets scaled to all N targets.
+    # its serial build plus the threaded walk of 16384 targets scaled to all N targets
+    # (the faster of two calls).
     rng = np.random.default_rng(0)
-    idx = rng.choice(n, size=2048, replace=False)
+    idx = rng.choice(n, size=16384, replace=False)
     for theta in (0.7, 0.5):
-        tt = [0.0, 0.0]
-        oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx], 0.1, theta,
-                                   nthreads=oracle.default_threads(), times=tt)
-        out[f"theta_{theta}"]["cpu_reference_s_per_step"] = tt[0] + tt[1] * n / idx.size
-        out[f"theta_{theta}"]["cpu_reference_build_s"] = tt[0]
+        best = None
+        for _ in range(2):
+            tt = [0.0, 0.0]
+            oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx], 0.1, theta,
+                                       nthreads=oracle.default_threads(), times=tt)
+            best = tt if best is None else [min(best[0], tt[0]), min(best[1], tt[1])]
+        out[f"theta_{theta}"]["cpu_reference_s_per_step"] = best[0] + best[1] * n / idx.size
+        out[f"theta_{theta}"]["cpu_reference_build_s"] = best[0]
+        out[f"theta_{theta}"]["cpu_reference_sample"] = f"build + walk of {idx.size} targets x N / {idx.size}"
         out[f"theta_{theta}"]["cpu_reference_cores"] = oracle.default_threads()
     return out
 
@@ -539,7 +544,7 @@ def report_config4(dev, n=16384):
     v0 = torch.from_numpy(ic["vel"]).to(dev)
     m = torch.from_numpy(ic["mass"]).to(dev)
     out = {"n": n}
-    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (200, 8, 20, (1e-9, 1e-11))):
+    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (200, 8, 20, (1e-9, 1e-11, 1e-12))):
         rng = np.random.default_rng(1)
         xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
         vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()

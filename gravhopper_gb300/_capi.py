@@ -80,6 +80,7 @@ SIGNATURES = {
     "gh_potential_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_dkd_backward_dev": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _vp, _vp, _vp, _vp]),
     "gh_direct_num_shapes": (_int, []),
+    "gh_direct_set_fp64_form": (_int, [_int]),
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),
     "gh_measure_l2_read": (_int, [_vp, _vp]),

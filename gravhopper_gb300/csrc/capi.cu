@@ -183,4 +183,9 @@ int gh_direct_set_shape(int shape) {
 
 int gh_direct_num_shapes(void) { return kNumMixedShapes; }
 
+int gh_direct_set_fp64_form(int form) {
+  clear_error();
+  return set_f64_form(form);
+}
+
 }  // extern "C"

@@ -100,6 +100,7 @@ static std::recursive_mutex g_mu;
 
 // Shape of the mixed kernel (index into kMixedShapes); -1 picks by problem size.
 static int g_mixed_shape = -1;
+static int g_f64_form = -1;  // -1 by target count, 0 thread per target, 1 ordered CTA-wide terms
 
 // Measured on GB300 (pairs/s per shape at N = 2000, 16384, 1048576): small systems
 // want small tiles (more CTAs share the sources), large ones the widest CTAs.
@@ -188,6 +189,12 @@ StreamK mixed_plan(int64_t np, int64_t nt, int64_t grid_cap, int tile, int jt) {
   return s;
 }
 
+int set_f64_form(int form) {
+  if (form < -1 || form > 1) return set_error(GH_ERR_ARG, "fp64 form %d out of range", form);
+  g_f64_form = form;
+  return GH_OK;
+}
+
 int set_mixed_shape(int shape) {
   if (shape < 0) shape = -1;
   if (shape >= kNumMixedShapes) return set_error(GH_ERR_ARG, "mixed shape %d out of range", shape);
@@ -252,9 +259,25 @@ static int launch_f64(const double* spos, const double* smass, int64_t np, const
   const int64_t per = F64_THREADS * F64_R;
   const int64_t blocks = (nt + per - 1) / per;
   if (blocks == 0) return GH_OK;
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  const int64_t want = 2LL * di.num_sms;  // CTAs for a full machine
+  int form = g_f64_form;
+  if (form < 0) form = blocks < want ? 1 : 0;
   prof_begin(st);
-  direct_f64_kernel<SELF, Epi><<<(unsigned)blocks, F64_THREADS, 0, st>>>(spos, smass, np, tpos, nt,
-                                                                         eps * eps, epi);
+  if (form == 0) {
+    direct_f64_kernel<SELF, Epi><<<(unsigned)blocks, F64_THREADS, 0, st>>>(spos, smass, np, tpos, nt,
+                                                                           eps * eps, epi);
+  } else if ((nt + 7) / 8 >= want) {
+    direct_f64_ordered_kernel<SELF, 8, Epi>
+        <<<(unsigned)((nt + 7) / 8), F64O_THREADS, 0, st>>>(spos, smass, np, tpos, nt, eps * eps, epi);
+  } else if ((nt + 3) / 4 >= want) {
+    direct_f64_ordered_kernel<SELF, 4, Epi>
+        <<<(unsigned)((nt + 3) / 4), F64O_THREADS, 0, st>>>(spos, smass, np, tpos, nt, eps * eps, epi);
+  } else {
+    direct_f64_ordered_kernel<SELF, 2, Epi>
+        <<<(unsigned)((nt + 1) / 2), F64O_THREADS, 0, st>>>(spos, smass, np, tpos, nt, eps * eps, epi);
+  }
   prof_end(st);
   GH_LAUNCH_CHECK();
   return GH_OK;

@@ -186,6 +186,73 @@ __global__ void __launch_bounds__(F64_THREADS)
     if (ti[r] < nt) epi(ti[r], ax[r], ay[r], az[r]);
 }
 
+// FP64 form for few targets (fewer than two CTAs of the kernel above per SM): the
+// pair terms (m_j d) inv are computed by all threads of the CTA into shared memory,
+// then summed in ascending j by one thread per (target, component), so the sums are
+// the reference's own.  A self pair contributes +0.0, which leaves every sum
+// unchanged: a round-to-nearest sum started at +0.0 is never -0.0.
+constexpr int F64O_THREADS = 256;
+
+template <bool SELF, int TB, class Epi>
+__global__ void __launch_bounds__(F64O_THREADS)
+    direct_f64_ordered_kernel(const double* __restrict__ spos, const double* __restrict__ smass, int64_t np,
+                              const double* __restrict__ tpos, int64_t nt, double eps2, Epi epi) {
+  static_assert(3 * TB <= 32, "the summing threads form one warp");
+  constexpr int F64O_JC = 1024 / TB;      // sources per chunk: 1024 pair terms per chunk
+  constexpr int F64O_JP = F64O_JC + 1;    // padded rows: the summing threads hit distinct banks
+  __shared__ dvec4 src[F64O_JC];
+  __shared__ double term[3 * TB][F64O_JP];
+  __shared__ double tp[TB][3];
+  __shared__ double res[3 * TB];
+  const int tid = threadIdx.x;
+  const int64_t t0 = (int64_t)blockIdx.x * TB;
+  if (tid < 3 * TB) {
+    const int64_t ti = t0 + tid / 3;
+    tp[tid / 3][tid % 3] = ti < nt ? tpos[3 * ti + tid % 3] : 0.0;
+  }
+  double sum = 0.0;  // threads < 3 TB: target tid / 3, component tid % 3
+  for (int64_t j0 = 0; j0 < np; j0 += F64O_JC) {
+    __syncthreads();
+    for (int k = tid; k < F64O_JC; k += F64O_THREADS) {
+      const int64_t j = j0 + k;
+      if (j < np) src[k] = make_dvec4(spos[3 * j], spos[3 * j + 1], spos[3 * j + 2], smass[j]);
+    }
+    __syncthreads();
+    const int jn = (np - j0) < F64O_JC ? (int)(np - j0) : F64O_JC;
+    for (int q = tid; q < TB * F64O_JC; q += F64O_THREADS) {
+      const int t = q / F64O_JC, k = q % F64O_JC;
+      if (k >= jn) continue;
+      double vx = 0.0, vy = 0.0, vz = 0.0;
+      if (!(SELF && j0 + k == t0 + t)) {
+        const dvec4 s = src[k];
+        const double dx = dsub(s.x, tp[t][0]);
+        const double dy = dsub(s.y, tp[t][1]);
+        const double dz = dsub(s.z, tp[t][2]);
+        double r2 = dmul(dx, dx);
+        r2 = dadd(r2, dmul(dy, dy));
+        r2 = dadd(r2, dmul(dz, dz));
+        const double ss = dadd(r2, eps2);
+        double inv = ddiv(ddiv(1.0, ss), dsqrt(ss));
+        if (!SELF && ss == 0.0) inv = 0.0;
+        vx = dmul(dmul(s.w, dx), inv);
+        vy = dmul(dmul(s.w, dy), inv);
+        vz = dmul(dmul(s.w, dz), inv);
+      }
+      term[3 * t + 0][k] = vx;
+      term[3 * t + 1][k] = vy;
+      term[3 * t + 2][k] = vz;
+    }
+    __syncthreads();
+    if (tid < 3 * TB) {
+      const double* row = term[tid];
+      for (int k = 0; k < jn; k++) sum = dadd(sum, row[k]);
+    }
+  }
+  if (tid < 3 * TB) res[tid] = sum;
+  __syncthreads();
+  if (tid < TB && t0 + tid < nt) epi(t0 + tid, res[3 * tid], res[3 * tid + 1], res[3 * tid + 2]);
+}
+
 // ---------------------------------------------------------------------------
 // Mixed form: FP32 pair arithmetic on coordinates relative to an origin, f32x2
 // packed over pairs of targets, per-chunk FP32 partial sums folded into a

@@ -13,6 +13,7 @@ int direct_force(const double* pos, const double* mass, int64_t np, const double
 
 // Selects the tile shape of the mixed direct kernel (index into kMixedShapes).
 int set_mixed_shape(int shape);
+int set_f64_form(int form);
 
 // `nsteps` leapfrog steps with the direct force, one fused launch per step.
 int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt,

@@ -125,6 +125,12 @@ int gh_direct_mixed_noalloc(const double* pos, const double* mass, int64_t np, d
 int gh_direct_set_shape(int shape);
 int gh_direct_num_shapes(void);
 
+/* Selects the FP64 direct kernel for all later calls in this process: 0 one thread
+ * per target, 1 CTA-wide pair terms summed in order per target (for few targets),
+ * -1 (the default) by target count.  Both give the reference's bits.  No counterpart
+ * in the reference. */
+int gh_direct_set_fp64_form(int form);
+
 /* ---- adjoint and diagnostics of the direct sum (no counterpart in the reference) ---- */
 
 /* Vector-Jacobian product of the direct-sum self-acceleration a(x, m) (code units):

@@ -115,3 +115,27 @@ def test_throughput_probes(lib, cuda):
     assert 1e12 < f32 < 1e15 and 1e10 < f64 < f32
     l2 = _capi.measure_l2_read()
     assert 1e12 < l2 < 1e15
+
+
+@pytest.mark.parametrize("form", [0, 1])
+def test_fp64_forms_bit_exact(lib, cuda, form):
+    """Both FP64 kernels (thread per target; CTA-wide terms summed in order) give the
+    reference's bits, for self forces, target points and zero softening."""
+    from gravhopper_gb300 import _capi, _jbgrav, ics
+    ic = ics.plummer(3001, seed=12)
+    rng = np.random.default_rng(2)
+    fp = np.concatenate([ic["pos"][:7], rng.normal(size=(300, 3)) * 1e-3])
+    _capi.call("gh_direct_set_fp64_form", form)
+    try:
+        for n in (3001, 2000, 300):  # 8, 4 and 2 targets per CTA on 152 SMs
+            p, m = ic["pos"][:n], ic["mass"][:n]
+            np.testing.assert_array_equal(_jbgrav.direct_summation(p, m, 5e-5),
+                                          oracle.direct_summation(p, m, 5e-5))
+        np.testing.assert_array_equal(_jbgrav.direct_summation_position(ic["pos"], ic["mass"], fp, 0.0),
+                                      oracle.direct_summation_position(ic["pos"], ic["mass"], fp, 0.0))
+        for nt in (1, 5, 9, 77):  # target counts around the CTA widths 2, 4 and 8
+            np.testing.assert_array_equal(
+                _jbgrav.direct_summation_position(ic["pos"], ic["mass"], fp[:nt], 5e-5),
+                oracle.direct_summation_position(ic["pos"], ic["mass"], fp[:nt], 5e-5))
+    finally:
+        _capi.call("gh_direct_set_fp64_form", -1)
