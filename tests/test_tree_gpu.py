@@ -69,15 +69,30 @@ def test_tree_deep_levels_widen_keys(lib, cuda):
 def test_tree_dense_clumps(lib, cuda, clumps, per_clump):
     """Clumps of side 1e-8 in a unit box share their first 21 levels: runs of up to
     256 equal first key words are ordered in place, a longer run takes the full
-    multi-word sort."""
-    from gravhopper_gb300 import _jbgrav
+    multi-word sort.  At theta = 0 (every leaf, no internal monopole) the forces and
+    the number of cells match the reference tree tightly.  At theta > 0 the internal
+    monopoles, summed in another order, differ from the reference's by ~1e-16 of the
+    clump's distance from the origin, i.e. ~1e-8 of the clump's own size, and the
+    forces inside a clump by as much: rms <= 1e-7, max <= 1e-6 there."""
+    from gravhopper_gb300 import _capi, _jbgrav
     rng = np.random.default_rng(6)
     centres = rng.uniform(-1, 1, size=(clumps, 1, 3))
     pos = (centres + 1e-8 * rng.uniform(0, 1, size=(clumps, per_clump, 3))).reshape(-1, 3)
     pos = np.concatenate([pos, rng.uniform(-1, 1, size=(200, 3))])
     m = rng.uniform(1, 2, size=len(pos))
+    ref, ncells = oracle.tree_force(pos, m, 1e-10, 0.0, return_nodes=True)
+    _capi.tree_stats_read()
+    _capi.tree_stats(True)
+    try:
+        got = _jbgrav.tree_force(pos, m, 1e-10, 0.0)
+        c = _capi.tree_stats_read()
+    finally:
+        _capi.tree_stats(False)
+    check(got, ref)
+    assert c["target_visits"] == len(pos) * ncells
     for theta in (0.5, 0.7):
-        check(_jbgrav.tree_force(pos, m, 1e-10, theta), oracle.tree_force(pos, m, 1e-10, theta))
+        check(_jbgrav.tree_force(pos, m, 1e-10, theta), oracle.tree_force(pos, m, 1e-10, theta),
+              rms_tol=1e-7, max_tol=1e-6)
 
 
 def test_tree_coincident_particles_error(lib, cuda):
@@ -181,9 +196,8 @@ def test_tree_walk_counters(lib, cuda):
     finally:
         _capi.tree_stats(False)
     assert c0["walks"] == 1 and c0["interactions"] == n * n
-    assert c0["target_visits"] % n == 0
-    ncells = c0["target_visits"] // n
-    assert ncells > n
+    _, ncells = oracle.tree_force(ic["pos"], ic["mass"], 5e-5, 0.0, return_nodes=True)
+    assert c0["target_visits"] == n * ncells
     assert c0["cell_steps"] == (n + 31) // 32 * ncells
     assert c7["walks"] == 1
     assert 0 < c7["interactions"] < c7["target_visits"] < c0["target_visits"]
