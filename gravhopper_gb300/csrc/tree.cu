@@ -5,7 +5,8 @@
 //   1. bounding box and root cell with the reference's boxsize rule (_jbgrav.c:747-775);
 //   2. per-particle octant keys: at each level the octant is (x>cx, y>cy, z>cz) and the
 //      child centre is c + (+-0.5*halfsize), the same FP64 recurrence as
-//      gravoct_calc_subnode / gravoct_add_particle (_jbgrav.c:403-428, 453-462).
+//      gravoct_calc_subnode / gravoct_add_particle (_jbgrav.c:403-428, 453-462); read
+//      off the bits of (p - c_0)/size wherever that provably gives the same decisions.
 //      21 levels per 64-bit word, MSB first, digit = x | y<<1 | z<<2 (the reference's
 //      branch number, _jbgrav.c:441-450), so key order is depth-first order with
 //      children in branch order 0..7.  The number of words grows until no two
@@ -14,12 +15,13 @@
 //      words ordered by the other words (a full multi-word radix sort for long runs);
 //   4. the node set of the reference's uncompressed octree (every cell that holds a
 //      particle and whose parent holds at least two, single-child chains included)
-//      laid out in depth-first preorder with skip ("next") indices, from the common
-//      prefix lengths of neighbouring keys;
-//   5. monopole pass: leaves take the particle's position and mass exactly
-//      (gravoct_finalize, _jbgrav.c:467-483); internal cells sum their children's
-//      mass and first moment (the reference sums per particle in insertion order, so
-//      the last bits of an internal COM can differ) and divide.
+//      laid out in depth-first preorder with skip ("next") indices and parent links,
+//      from the common prefix lengths of neighbouring keys;
+//   5. monopole pass, one launch bottom-up: leaves take the particle's position and
+//      mass exactly (gravoct_finalize, _jbgrav.c:467-483); the last child to finish
+//      sums its cell's children's mass and first moment (the reference sums per
+//      particle in insertion order, so the last bits of an internal COM can differ)
+//      and divides.
 // Walk: one warp per 32 consecutive targets in key order.  Each lane applies the
 // reference's test "leaf or size/|center - x| < theta" (_jbgrav.c:496-502) to every
 // cell its own traversal reaches; the warp visits the union of those cells in
@@ -45,6 +47,8 @@ constexpr double TREE_MARGIN = 1e-4;
 struct TreeRoot {
   double c[3];
   double size;
+  double inv;           // RN(1 / size)
+  long long margin;     // 0: fast keys allowed; -1: the FP64 recurrence for every particle
 };
 
 // ---------------------------------------------------------------------------
@@ -107,30 +111,64 @@ __global__ void __launch_bounds__(BB_THREADS)
 
 // treeforce_workhorse, _jbgrav.c:764-772: boxsize = extent_x + eps, replaced by
 // extent_i + eps when extent_i (without eps) exceeds it; centre = bbox midpoint.
+// One warp folds the per-block partial boxes.
+//
+// Fast keys.  The reference's cell centres follow c_{l+1} = RN(c_l +- size 2^-(l+2)).
+// Along a particle's own path the level-(l+1) centre lies within size 2^-(l+2) of p,
+// so that rounding moves it by at most 2^-53 (|p| + size 2^-(l+2)), and after 42
+// levels the centre is within E_c = 2^-53 (42 |p| + size/2) of the exact dyadic
+// centre (per axis).  With t = (p - c_0) / size + 1/2 computed as
+// fma(p - c_0, RN(1/size), 1/2) (error below 2^-52), each of the first 42 octant
+// decisions "p > c_l" equals the bit of t at that level unless t lies within
+// E_c / size + 2^-52 of a multiple of 2^-42.  keys_kernel keeps that window, doubled,
+// in units of 2^-63; particles inside it take the reference's FP64 recurrence, as do
+// all particles when the box size is outside [2^-900, 2^900] (margin -1).
 __global__ void root_kernel(const double* __restrict__ part, int nb, double eps, TreeRoot* __restrict__ root) {
-  if (threadIdx.x || blockIdx.x) return;
-  double mn[3], mx[3];
-  for (int k = 0; k < 3; k++) {
-    mn[k] = part[k];
-    mx[k] = part[3 + k];
-  }
-  for (int b = 1; b < nb; b++)
+  if (blockIdx.x) return;
+  const int lane = threadIdx.x;
+  const double inf = __longlong_as_double(0x7ff0000000000000ll);
+  double mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf};
+  for (int b = lane; b < nb; b += 32)
     for (int k = 0; k < 3; k++) {
-      double a = part[6 * b + k], c = part[6 * b + 3 + k];
+      const double a = part[6 * b + k], c = part[6 * b + 3 + k];
       if (a < mn[k]) mn[k] = a;
       if (c > mx[k]) mx[k] = c;
     }
+  for (int o = 16; o > 0; o >>= 1)
+    for (int k = 0; k < 3; k++) {
+      const double a = __shfl_xor_sync(0xffffffffu, mn[k], o), c = __shfl_xor_sync(0xffffffffu, mx[k], o);
+      if (a < mn[k]) mn[k] = a;
+      if (c > mx[k]) mx[k] = c;
+    }
+  if (lane) return;
   double bs = dadd(dsub(mx[0], mn[0]), eps);
   for (int k = 1; k < 3; k++)
     if (dsub(mx[k], mn[k]) > bs) bs = dadd(dsub(mx[k], mn[k]), eps);
-  for (int k = 0; k < 3; k++) root->c[k] = dmul(0.5, dadd(mn[k], mx[k]));
+  double amax = 0.0;
+  for (int k = 0; k < 3; k++) {
+    root->c[k] = dmul(0.5, dadd(mn[k], mx[k]));
+    amax = fmax(amax, fabs(root->c[k]));
+  }
   root->size = bs;
+  root->inv = ddiv(1.0, bs);
+  root->margin = (bs > 0x1p-900 && bs < 0x1p+900 && amax < 0x1p+900) ? 0 : -1;
 }
 
 // ---------------------------------------------------------------------------
 // 2. Octant keys
 // ---------------------------------------------------------------------------
 constexpr int TREE_MAX_LEVELS = KEY_LEVELS * TREE_MAX_WORDS;
+
+// Spreads the low 21 bits of v to every third bit (bit b to bit 3b).
+__device__ __forceinline__ uint64_t spread3(uint64_t v) {
+  v &= 0x1fffffull;
+  v = (v | (v << 32)) & 0x001f00000000ffffull;
+  v = (v | (v << 16)) & 0x001f0000ff0000ffull;
+  v = (v | (v << 8)) & 0x100f00f00f00f00full;
+  v = (v | (v << 4)) & 0x10c30c30c30c30c3ull;
+  v = (v | (v << 2)) & 0x1249249249249249ull;
+  return v;
+}
 
 __global__ void keys_kernel(const double* __restrict__ pos, int64_t n, const TreeRoot* __restrict__ root,
                             int words, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
@@ -147,14 +185,35 @@ __global__ void keys_kernel(const double* __restrict__ pos, int64_t n, const Tre
   __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const double p0 = pos[3 * i], p1 = pos[3 * i + 1], p2 = pos[3 * i + 2];
+  idx[i] = (uint32_t)i;
+  const double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
+  if (root->margin >= 0 && words == 2) {
+    uint64_t T[3];
+    bool ok = true;
+    const double inv = root->inv;
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      const double t = fma(dsub(p[k], root->c[k]), inv, 0.5);
+      T[k] = t >= 1.0 ? (1ull << 63) : (t > 0.0 ? (uint64_t)(t * 0x1p63) : 0ull);
+      // 2 * 2^63 * (E_c / size + 2^-52) + slack, in FP32 (a bound, not a value)
+      const float mf = fmaf(86016.f * 1.01f * fabsf((float)p[k]), (float)inv, 5200.f);
+      const uint64_t r = T[k] & ((1ull << 21) - 1);
+      ok = ok && mf < 1048576.f && r > (uint64_t)mf && r < (1ull << 21) - (uint64_t)mf;
+    }
+    if (ok) {
+      keys[i] = spread3(T[0] >> 42) | (spread3(T[1] >> 42) << 1) | (spread3(T[2] >> 42) << 2);
+      keys[n + i] = spread3(T[0] >> 21) | (spread3(T[1] >> 21) << 1) | (spread3(T[2] >> 21) << 2);
+      return;
+    }
+  }
+  // the reference's recurrence (gravoct_calc_subnode, _jbgrav.c:441-462)
   double c0 = root->c[0], c1 = root->c[1], c2 = root->c[2];
   for (int w = 0; w < words; w++) {
     uint64_t k = 0;
 #pragma unroll 3
     for (int l = 0; l < KEY_LEVELS; l++) {
       const double off = offs[w * KEY_LEVELS + l];
-      const unsigned g0 = p0 > c0, g1 = p1 > c1, g2 = p2 > c2;
+      const unsigned g0 = p[0] > c0, g1 = p[1] > c1, g2 = p[2] > c2;
       c0 = g0 ? dadd(c0, off) : dsub(c0, off);
       c1 = g1 ? dadd(c1, off) : dsub(c1, off);
       c2 = g2 ? dadd(c2, off) : dsub(c2, off);
@@ -162,7 +221,6 @@ __global__ void keys_kernel(const double* __restrict__ pos, int64_t n, const Tre
     }
     keys[(int64_t)w * n + i] = k;
   }
-  idx[i] = (uint32_t)i;
 }
 
 __device__ __forceinline__ int key_lcp(const uint64_t* __restrict__ keys, int words, int64_t n, int64_t a,
@@ -285,45 +343,96 @@ struct __align__(64) WalkRec {
 
 struct NodeArrays {
   WalkRec* R;    // walk records (A, L, Mh, Ml)
-  dvec4* C;      // (cx, cy, cz, size)                    exact opening test
+  dvec4* C;      // (cx, cy, cz, size)                    exact opening test (internal cells)
   dvec4* M;      // (comx, comy, comz, mass)              interaction
   dvec4* F;      // (first moment x, y, z, mass)          build only
-  int* first;    // first particle (sorted position)
-  int* level;
+  int* parent;   // enclosing cell, -1 for the root        build only
+  int* nchild;   // number of child cells                  build only
+  int* arrive;   // children whose monopole is done        build only
 };
 
 __device__ __forceinline__ float f32_hi(double v) { return (float)v; }
 __device__ __forceinline__ float f32_lo(double v, float hi) { return (float)(v - (double)hi); }
 
+// First particle after i that shares fewer than L leading digits with it: a short
+// scan of the neighbour prefixes, then a binary search on the keys.
+__device__ __forceinline__ int64_t cell_end(const uint64_t* __restrict__ keys, int words, int64_t n,
+                                            const int* __restrict__ lp, int64_t i, int L) {
+  int64_t j = i + 1;
+  for (int s = 0; s < 16; s++, j++)
+    if (lp[j] < L) return j;  // lp[n] = -1 ends the scan
+  int64_t a = j - 1, b = n - 1;  // a shares >= L digits with i
+  while (a < b) {
+    const int64_t mid = (a + b + 1) >> 1;
+    if (key_lcp(keys, words, n, i, mid) >= L)
+      a = mid;
+    else
+      b = mid - 1;
+  }
+  return a + 1;
+}
+
+// First particle of the level-L cell that holds particle i (L <= lp[i]).
+__device__ __forceinline__ int64_t cell_begin(const uint64_t* __restrict__ keys, int words, int64_t n,
+                                              const int* __restrict__ lp, int64_t i, int L) {
+  int64_t j = i;
+  for (int s = 0; s < 16; s++, j--)
+    if (lp[j] < L) return j;  // lp[0] = -1 ends the scan
+  int64_t a = 0, b = j;  // b shares >= L digits with i
+  while (a < b) {
+    const int64_t mid = (a + b) >> 1;
+    if (key_lcp(keys, words, n, mid, i) >= L)
+      b = mid;
+    else
+      a = mid + 1;
+  }
+  return a;
+}
+
+// Particle i opens the cells at levels lo = lp[i]+1 .. d (its leaf), nodes
+// base[i] .. base[i] + d - lo in preorder.  Each cell records its enclosing cell and
+// counts itself there.  Internal cells get their centre from the reference's FP64
+// recurrence along i's digits (gravoct_add_particle, _jbgrav.c:403-428); a leaf is
+// always accepted by the walk, so only its skip index is needed.
 __global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
                              const int* __restrict__ lp, const int* __restrict__ depth,
                              const int* __restrict__ base, const TreeRoot* __restrict__ root, NodeArrays na,
                              int nnodes) {
+  __shared__ double offs[TREE_MAX_LEVELS];  // size 2^-(L+2), exact
+  const double S = root->size;
+  for (int l = threadIdx.x; l < TREE_MAX_LEVELS; l += blockDim.x)
+    offs[l] = dmul(S, __longlong_as_double((long long)(1023 - (l + 2)) << 52));
+  __syncthreads();
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const int lo = lp[i] + 1, d = depth[i];
   const int k0 = base[i];
+  int par = -1;
+  if (lo > 0) {
+    const int64_t j0 = cell_begin(keys, words, n, lp, i, lo - 1);
+    par = base[j0] + (lo - 1) - (lp[j0] + 1);
+  }
+  for (int L = lo; L <= d; L++) {
+    const int k = k0 + (L - lo);
+    const int pk = L == lo ? par : k - 1;
+    na.parent[k] = pk;
+    if (pk >= 0) atomicAdd(&na.nchild[pk], 1);
+  }
+  // leaf: skip index only
+  {
+    const int k = k0 + (d - lo);
+    const int next = i + 1 < n ? base[i + 1] : nnodes;
+    na.R[k].A = make_float4(0.f, 0.f, 0.f, 0.f);
+    na.R[k].L = make_float4(0.f, 0.f, 0.f, __int_as_float(next));
+  }
+  if (d == lo) return;
   double c[3] = {root->c[0], root->c[1], root->c[2]};
-  double size = root->size;
-  for (int L = 0; L <= d; L++) {
+  for (int L = 0; L < d; L++) {
     if (L >= lo) {
       const int k = k0 + (L - lo);
-      int64_t end;
-      if (L == d) {
-        end = i + 1;
-      } else {
-        // last particle sharing the first L digits with i
-        int64_t a = i, b = n - 1;
-        while (a < b) {
-          int64_t mid = (a + b + 1) >> 1;
-          if (key_lcp(keys, words, n, i, mid) >= L)
-            a = mid;
-          else
-            b = mid - 1;
-        }
-        end = a + 1;
-      }
+      const int64_t end = cell_end(keys, words, n, lp, i, L);
       const int next = end < n ? base[end] : nnodes;
+      const double size = dmul(S, __longlong_as_double((long long)(1023 - L) << 52));
       float4 A, Lo;
       A.x = f32_hi(c[0]);
       A.y = f32_hi(c[1]);
@@ -336,64 +445,23 @@ __global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64
       na.R[k].A = A;
       na.R[k].L = Lo;
       na.C[k] = make_dvec4(c[0], c[1], c[2], size);
-      na.first[k] = (int)i;
-      na.level[k] = L;
     }
-    if (L < d) {
+    if (L + 1 < d) {
       const unsigned g = key_digit(keys, n, i, L);
-      const double hs = dmul(0.5, size);
-      const double off = dmul(0.5, hs);
+      const double off = offs[L];
 #pragma unroll
       for (int q = 0; q < 3; q++) c[q] = ((g >> q) & 1u) ? dadd(c[q], off) : dsub(c[q], off);
-      size = hs;
     }
   }
 }
 
 // ---------------------------------------------------------------------------
-// 5. Monopole pass, deepest level first
+// 5. Monopole pass, bottom-up in one launch
 // ---------------------------------------------------------------------------
-// Warp-aggregated: lanes with the same level add once per warp (a few dozen levels
-// would otherwise serialise a million atomics on a few addresses).
-__device__ __forceinline__ unsigned lanemask_lt_tree() {
-  unsigned m;
-  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
-  return m;
-}
-
-__global__ void level_hist_kernel(const int* __restrict__ level, int nnodes, int* __restrict__ hist) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int l = k < nnodes ? level[k] : -1;
-  const unsigned peers = __match_any_sync(0xffffffffu, l);
-  if (l >= 0 && (peers & lanemask_lt_tree()) == 0) atomicAdd(&hist[l], __popc(peers));
-}
-
-// hist (levels+1 entries) -> off (exclusive prefix) and cursor (= off)
-__global__ void level_scan_kernel(const int* __restrict__ hist, int levels, int* __restrict__ off,
-                                  int* __restrict__ cursor) {
-  if (threadIdx.x || blockIdx.x) return;
-  int s = 0;
-  for (int l = 0; l < levels; l++) {
-    off[l] = s;
-    cursor[l] = s;
-    s += hist[l];
-  }
-  off[levels] = s;
-}
-
-__global__ void level_scatter_kernel(const int* __restrict__ level, int nnodes, int* __restrict__ cursor,
-                                     int* __restrict__ bucket) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  const int l = k < nnodes ? level[k] : -1;
-  const unsigned peers = __match_any_sync(0xffffffffu, l);
-  const int leader = __ffs(peers) - 1;
-  const int rank = __popc(peers & lanemask_lt_tree());
-  int base = 0;
-  if (l >= 0 && rank == 0) base = atomicAdd(&cursor[l], __popc(peers));
-  base = __shfl_sync(0xffffffffu, base, leader);
-  if (l >= 0) bucket[base + rank] = k;
-}
-
+// Each particle sets its leaf (gravoct_finalize, _jbgrav.c:467-483: the particle's own
+// position and mass) and climbs: the child that arrives last at a cell (per-cell
+// counter) sums the cell's children in preorder and climbs on.  The sums do not
+// depend on which child arrives last, so the result is deterministic.
 __device__ __forceinline__ int node_next(const WalkRec* __restrict__ R, int k) { return __float_as_int(R[k].L.w); }
 
 // FP32 hi/lo split of a cell's centre of mass, for the mixed-precision walk.
@@ -404,37 +472,41 @@ __device__ __forceinline__ void store_mixed_com(const NodeArrays& na, int k, dou
   na.R[k].Ml = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), 0.f);
 }
 
-__global__ void com_leaf_kernel(NodeArrays na, int nnodes, const uint32_t* __restrict__ perm,
-                                const double* __restrict__ pos, const double* __restrict__ mass) {
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= nnodes || node_next(na.R, k) != k + 1) return;
-  const int64_t p = perm[na.first[k]];
-  const double m = mass[p];
-  const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
-  na.M[k] = make_dvec4(x, y, z, m);
-  na.F[k] = make_dvec4(dmul(m, x), dmul(m, y), dmul(m, z), m);
-  store_mixed_com(na, k, x, y, z, m);
-}
-
-__global__ void com_level_kernel(NodeArrays na, const int* __restrict__ bucket, const int* __restrict__ off,
-                                 int level) {
-  const int b0 = off[level], b1 = off[level + 1];
-  for (int t = b0 + blockIdx.x * blockDim.x + threadIdx.x; t < b1; t += gridDim.x * blockDim.x) {
-    const int k = bucket[t];
-    const int nx = node_next(na.R, k);
-    if (nx == k + 1) continue;  // leaf
+__global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ lp, const int* __restrict__ depth,
+                              const int* __restrict__ base, const uint32_t* __restrict__ perm,
+                              const double* __restrict__ pos, const double* __restrict__ mass) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  int cur = base[i] + (depth[i] - (lp[i] + 1));
+  {
+    const int64_t p = perm[i];
+    const double m = mass[p];
+    const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
+    na.M[cur] = make_dvec4(x, y, z, m);
+    na.F[cur] = make_dvec4(dmul(m, x), dmul(m, y), dmul(m, z), m);
+    store_mixed_com(na, cur, x, y, z, m);
+  }
+  for (;;) {
+    const int par = na.parent[cur];
+    if (par < 0) break;
+    __threadfence();  // this child's moments before its arrival
+    if (atomicAdd(&na.arrive[par], 1) != na.nchild[par] - 1) break;
+    __threadfence();  // every sibling's moments after the last arrival
+    const int nx = node_next(na.R, par);
     double fx = 0.0, fy = 0.0, fz = 0.0, m = 0.0;
-    for (int c = k + 1; c < nx; c = node_next(na.R, c)) {
-      const dvec4 f = na.F[c];
-      fx = dadd(fx, f.x);
-      fy = dadd(fy, f.y);
-      fz = dadd(fz, f.z);
-      m = dadd(m, f.w);
+    for (int c = par + 1; c < nx; c = node_next(na.R, c)) {
+      const double2* f = reinterpret_cast<const double2*>(na.F + c);
+      const double2 fa = __ldcg(f), fb = __ldcg(f + 1);  // siblings were written by other threads
+      fx = dadd(fx, fa.x);
+      fy = dadd(fy, fa.y);
+      fz = dadd(fz, fb.x);
+      m = dadd(m, fb.y);
     }
-    na.F[k] = make_dvec4(fx, fy, fz, m);
+    na.F[par] = make_dvec4(fx, fy, fz, m);
     const double cx = ddiv(fx, m), cy = ddiv(fy, m), cz = ddiv(fz, m);
-    na.M[k] = make_dvec4(cx, cy, cz, m);
-    store_mixed_com(na, k, cx, cy, cz, m);
+    na.M[par] = make_dvec4(cx, cy, cz, m);
+    store_mixed_com(na, par, cx, cy, cz, m);
+    cur = par;
   }
 }
 
@@ -593,9 +665,10 @@ __global__ void __launch_bounds__(TW_THREADS)
 // ---------------------------------------------------------------------------
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
-  Buffer nA, nC, nM, nF, first, level, lvl_hist, lvl_off, lvl_cursor, bucket, xh[2];
+  Buffer nA, nC, nM, nF, parent, nchild, arrive, xh[2];
   int* host_flags = nullptr;  // pinned: tie, maxdepth, long run, nnodes
   int words = TREE_MIN_WORDS;
+  int64_t full_sort_n = -1;  // particle count whose last build needed the full multi-word sort
 };
 static TreeWS g_tree[64];
 static std::recursive_mutex g_tree_mu;
@@ -606,8 +679,9 @@ static NodeArrays node_arrays(TreeWS& ws) {
   na.C = (dvec4*)ws.nC.ptr;
   na.M = (dvec4*)ws.nM.ptr;
   na.F = (dvec4*)ws.nF.ptr;
-  na.first = (int*)ws.first.ptr;
-  na.level = (int*)ws.level.ptr;
+  na.parent = (int*)ws.parent.ptr;
+  na.nchild = (int*)ws.nchild.ptr;
+  na.arrive = (int*)ws.arrive.ptr;
   return na;
 }
 
@@ -643,7 +717,9 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.idx_tmp, n * sizeof(uint32_t)));
   GH_TRY(ensure(ws.rs, radix_scratch_words(n) * sizeof(uint32_t)));
   // 2-3. keys, sort, prefix structure; widen the keys while particles tie
-  bool full_sort = false;
+  // A long run of equal first words usually recurs in the next build of the same
+  // system (a stepping loop), so the full sort is kept for that particle count.
+  bool full_sort = ws.full_sort_n == n;
   for (;;) {
     const int words = ws.words;
     GH_TRY(ensure(ws.keys, (size_t)words * n * sizeof(uint64_t)));
@@ -680,6 +756,7 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
     GH_CUDA_TRY(cudaStreamSynchronize(st));
     if (ws.host_flags[2] && !full_sort) {  // a long run of equal first words
       full_sort = true;
+      ws.full_sort_n = n;
       continue;
     }
     if (!ws.host_flags[0]) break;
@@ -697,33 +774,19 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nM, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nF, (size_t)nnodes * sizeof(dvec4)));
-  GH_TRY(ensure(ws.first, (size_t)nnodes * sizeof(int)));
-  GH_TRY(ensure(ws.level, (size_t)nnodes * sizeof(int)));
+  GH_TRY(ensure(ws.parent, (size_t)nnodes * sizeof(int)));
+  GH_TRY(ensure(ws.nchild, (size_t)nnodes * sizeof(int)));
+  GH_TRY(ensure(ws.arrive, (size_t)nnodes * sizeof(int)));
   NodeArrays na = node_arrays(ws);
+  GH_CUDA_TRY(cudaMemsetAsync(ws.nchild.ptr, 0, (size_t)nnodes * sizeof(int), st));
+  GH_CUDA_TRY(cudaMemsetAsync(ws.arrive.ptr, 0, (size_t)nnodes * sizeof(int), st));
   nodes_kernel<<<gn, T, 0, st>>>((const uint64_t*)ws.keys.ptr, words, n, (const int*)ws.lp.ptr,
                                  (const int*)ws.depth.ptr, (const int*)ws.base.ptr, root, na, nnodes);
   GH_LAUNCH_CHECK();
-  // 5. monopoles, by level
-  const int levels = maxdepth + 1;
-  GH_TRY(ensure(ws.lvl_hist, (levels + 1) * sizeof(int)));
-  GH_TRY(ensure(ws.lvl_off, (levels + 1) * sizeof(int)));
-  GH_TRY(ensure(ws.lvl_cursor, (levels + 1) * sizeof(int)));
-  GH_TRY(ensure(ws.bucket, (size_t)nnodes * sizeof(int)));
-  GH_CUDA_TRY(cudaMemsetAsync(ws.lvl_hist.ptr, 0, (levels + 1) * sizeof(int), st));
-  const unsigned gk = (unsigned)((nnodes + T - 1) / T);
-  level_hist_kernel<<<gk, T, 0, st>>>(na.level, nnodes, (int*)ws.lvl_hist.ptr);
+  // 5. monopoles
+  com_up_kernel<<<gn, T, 0, st>>>(na, n, (const int*)ws.lp.ptr, (const int*)ws.depth.ptr, (const int*)ws.base.ptr,
+                                  (const uint32_t*)ws.idx.ptr, pos, mass);
   GH_LAUNCH_CHECK();
-  level_scan_kernel<<<1, 32, 0, st>>>((const int*)ws.lvl_hist.ptr, levels, (int*)ws.lvl_off.ptr,
-                                      (int*)ws.lvl_cursor.ptr);
-  GH_LAUNCH_CHECK();
-  level_scatter_kernel<<<gk, T, 0, st>>>(na.level, nnodes, (int*)ws.lvl_cursor.ptr, (int*)ws.bucket.ptr);
-  GH_LAUNCH_CHECK();
-  com_leaf_kernel<<<gk, T, 0, st>>>(na, nnodes, (const uint32_t*)ws.idx.ptr, pos, mass);
-  GH_LAUNCH_CHECK();
-  for (int l = maxdepth - 1; l >= 0; l--) {
-    com_level_kernel<<<2 * 152, T, 0, st>>>(na, (const int*)ws.bucket.ptr, (const int*)ws.lvl_off.ptr, l);
-    GH_LAUNCH_CHECK();
-  }
   out->nnodes = nnodes;
   out->maxdepth = maxdepth;
   return GH_OK;

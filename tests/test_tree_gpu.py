@@ -95,6 +95,27 @@ def test_tree_dense_clumps(lib, cuda, clumps, per_clump):
               rms_tol=1e-7, max_tol=1e-6)
 
 
+def test_tree_lattice_on_cell_centres(lib, cuda):
+    """A lattice puts particles exactly on cell centres and faces, where the octant
+    test's ties go low (_jbgrav.c:441-450) and the keys take the FP64 recurrence."""
+    from gravhopper_gb300 import _capi, _jbgrav
+    g = np.arange(12) / 8.0
+    pos = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    m = np.ones(len(pos))
+    ref, ncells = oracle.tree_force(pos, m, 0.01, 0.0, return_nodes=True)
+    _capi.tree_stats_read()
+    _capi.tree_stats(True)
+    try:
+        got = _jbgrav.tree_force(pos, m, 0.01, 0.0)
+        c = _capi.tree_stats_read()
+    finally:
+        _capi.tree_stats(False)
+    check(got, ref)
+    assert c["target_visits"] == len(pos) * ncells
+    for theta in (0.5, 0.7):
+        check(_jbgrav.tree_force(pos, m, 0.01, theta), oracle.tree_force(pos, m, 0.01, theta))
+
+
 def test_tree_coincident_particles_error(lib, cuda):
     from gravhopper_gb300 import _capi, _jbgrav
     pos = np.array([[0.0, 0.0, 0.0], [1.0, 2.0, 3.0], [1.0, 2.0, 3.0]])
