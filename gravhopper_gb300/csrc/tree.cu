@@ -170,56 +170,86 @@ __device__ __forceinline__ uint64_t spread3(uint64_t v) {
   return v;
 }
 
+__device__ __forceinline__ unsigned lane_mask_lt() {
+  unsigned m;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(m));
+  return m;
+}
+
+// Appends i to list (warp-aggregated) where `need`; every lane of the warp calls it.
+__device__ __forceinline__ void warp_append(bool need, int64_t i, int* __restrict__ list, int* __restrict__ count) {
+  const unsigned mask = __ballot_sync(0xffffffffu, need);
+  if (!mask) return;
+  int base = 0;
+  if ((threadIdx.x & 31) == 0) base = atomicAdd(count, __popc(mask));
+  base = __shfl_sync(0xffffffffu, base, 0);
+  if (need) list[base + __popc(mask & lane_mask_lt())] = (int)i;
+}
+
+// Fast keys where the decisions are provably the recurrence's (see root_kernel);
+// the other particles are listed for keys_exact_kernel, so that the FP64 recurrence
+// runs on full warps.
 __global__ void keys_kernel(const double* __restrict__ pos, int64_t n, const TreeRoot* __restrict__ root,
-                            int words, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
-  // Child-centre offsets per level, the same for every particle: 0.5 * halfsize,
-  // halfsize halving each level (exact scalings of the root size).
-  __shared__ double offs[TREE_MAX_LEVELS];
-  if (threadIdx.x == 0) {
-    double hs = dmul(0.5, root->size);
-    for (int l = 0; l < words * KEY_LEVELS; l++) {
-      offs[l] = dmul(0.5, hs);
-      hs = dmul(0.5, hs);
-    }
-  }
-  __syncthreads();
+                            int words, uint64_t* __restrict__ keys, uint32_t* __restrict__ idx,
+                            int* __restrict__ list, int* __restrict__ count) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  idx[i] = (uint32_t)i;
-  const double p[3] = {pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]};
-  if (root->margin >= 0 && words == 2) {
-    uint64_t T[3];
-    bool ok = true;
-    const double inv = root->inv;
+  bool need = false;
+  if (i < n) {
+    idx[i] = (uint32_t)i;
+    need = true;
+    if (root->margin >= 0 && words == 2) {
+      uint64_t T[3];
+      bool ok = true;
+      const double inv = root->inv;
 #pragma unroll
-    for (int k = 0; k < 3; k++) {
-      const double t = fma(dsub(p[k], root->c[k]), inv, 0.5);
-      T[k] = t >= 1.0 ? (1ull << 63) : (t > 0.0 ? (uint64_t)(t * 0x1p63) : 0ull);
-      // 2 * 2^63 * (E_c / size + 2^-52) + slack, in FP32 (a bound, not a value)
-      const float mf = fmaf(86016.f * 1.01f * fabsf((float)p[k]), (float)inv, 5200.f);
-      const uint64_t r = T[k] & ((1ull << 21) - 1);
-      ok = ok && mf < 1048576.f && r > (uint64_t)mf && r < (1ull << 21) - (uint64_t)mf;
-    }
-    if (ok) {
-      keys[i] = spread3(T[0] >> 42) | (spread3(T[1] >> 42) << 1) | (spread3(T[2] >> 42) << 2);
-      keys[n + i] = spread3(T[0] >> 21) | (spread3(T[1] >> 21) << 1) | (spread3(T[2] >> 21) << 2);
-      return;
+      for (int k = 0; k < 3; k++) {
+        const double p = pos[3 * i + k];
+        const double t = fma(dsub(p, root->c[k]), inv, 0.5);
+        T[k] = t >= 1.0 ? (1ull << 63) : (t > 0.0 ? (uint64_t)(t * 0x1p63) : 0ull);
+        // 2 * 2^63 * (E_c / size + 2^-52) + slack, in FP32 (a bound, not a value)
+        const float mf = fmaf(86016.f * 1.01f * fabsf((float)p), (float)inv, 5200.f);
+        const uint64_t r = T[k] & ((1ull << 21) - 1);
+        ok = ok && mf < 1048576.f && r > (uint64_t)mf && r < (1ull << 21) - (uint64_t)mf;
+      }
+      if (ok) {
+        keys[i] = spread3(T[0] >> 42) | (spread3(T[1] >> 42) << 1) | (spread3(T[2] >> 42) << 2);
+        keys[n + i] = spread3(T[0] >> 21) | (spread3(T[1] >> 21) << 1) | (spread3(T[2] >> 21) << 2);
+        need = false;
+      }
     }
   }
-  // the reference's recurrence (gravoct_calc_subnode, _jbgrav.c:441-462)
-  double c0 = root->c[0], c1 = root->c[1], c2 = root->c[2];
-  for (int w = 0; w < words; w++) {
-    uint64_t k = 0;
+  warp_append(need, i, list, count);
+}
+
+// The reference's recurrence (gravoct_calc_subnode, _jbgrav.c:441-462) for the
+// listed particles.
+__global__ void keys_exact_kernel(const double* __restrict__ pos, int64_t n, const TreeRoot* __restrict__ root,
+                                  int words, uint64_t* __restrict__ keys, const int* __restrict__ list,
+                                  const int* __restrict__ count) {
+  // child-centre offsets 0.5 * halfsize = size 2^-(l+2), exact scalings of the root size
+  __shared__ double offs[TREE_MAX_LEVELS];
+  const double S = root->size;
+  for (int l = threadIdx.x; l < TREE_MAX_LEVELS; l += blockDim.x)
+    offs[l] = dmul(S, __longlong_as_double((long long)(1023 - (l + 2)) << 52));
+  __syncthreads();
+  const int cnt = *count;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+    const int64_t i = list[q];
+    const double p0 = pos[3 * i], p1 = pos[3 * i + 1], p2 = pos[3 * i + 2];
+    double c0 = root->c[0], c1 = root->c[1], c2 = root->c[2];
+    for (int w = 0; w < words; w++) {
+      uint64_t k = 0;
 #pragma unroll 3
-    for (int l = 0; l < KEY_LEVELS; l++) {
-      const double off = offs[w * KEY_LEVELS + l];
-      const unsigned g0 = p[0] > c0, g1 = p[1] > c1, g2 = p[2] > c2;
-      c0 = g0 ? dadd(c0, off) : dsub(c0, off);
-      c1 = g1 ? dadd(c1, off) : dsub(c1, off);
-      c2 = g2 ? dadd(c2, off) : dsub(c2, off);
-      k = (k << 3) | (uint64_t)(g0 | (g1 << 1) | (g2 << 2));
+      for (int l = 0; l < KEY_LEVELS; l++) {
+        const double off = offs[w * KEY_LEVELS + l];
+        const unsigned g0 = p0 > c0, g1 = p1 > c1, g2 = p2 > c2;
+        c0 = g0 ? dadd(c0, off) : dsub(c0, off);
+        c1 = g1 ? dadd(c1, off) : dsub(c1, off);
+        c2 = g2 ? dadd(c2, off) : dsub(c2, off);
+        k = (k << 3) | (uint64_t)(g0 | (g1 << 1) | (g2 << 2));
+      }
+      keys[(int64_t)w * n + i] = k;
     }
-    keys[(int64_t)w * n + i] = k;
   }
 }
 
@@ -267,6 +297,10 @@ __global__ void tie_rank_kernel(const uint64_t* __restrict__ keys, int words, in
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n || !tied_first_word(keys, n, i)) return;
   const uint64_t k = keys[i];
+  if ((i >= TIE_MAX_RUN && keys[i - TIE_MAX_RUN] == k) || (i + TIE_MAX_RUN < n && keys[i + TIE_MAX_RUN] == k)) {
+    atomicOr(&flags[2], 1);  // sorted keys: the run is longer than TIE_MAX_RUN
+    return;
+  }
   int64_t s = i, e = i + 1;
   while (s > 0 && keys[s - 1] == k) {
     if (i - --s >= TIE_MAX_RUN) {
@@ -390,67 +424,82 @@ __device__ __forceinline__ int64_t cell_begin(const uint64_t* __restrict__ keys,
 }
 
 // Particle i opens the cells at levels lo = lp[i]+1 .. d (its leaf), nodes
-// base[i] .. base[i] + d - lo in preorder.  Each cell records its enclosing cell and
-// counts itself there.  Internal cells get their centre from the reference's FP64
-// recurrence along i's digits (gravoct_add_particle, _jbgrav.c:403-428); a leaf is
-// always accepted by the walk, so only its skip index is needed.
+// base[i] .. base[i] + d - lo in preorder.  nodes_kernel records each cell's
+// enclosing cell (counting itself there) and the leaf's skip index, and lists the
+// particles that open internal cells; nodes_internal_kernel gives those cells their
+// centre from the reference's FP64 recurrence along the particle's digits
+// (gravoct_add_particle, _jbgrav.c:403-428) and their skip index.  A leaf is always
+// accepted by the walk, so it needs no centre.
 __global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
                              const int* __restrict__ lp, const int* __restrict__ depth,
-                             const int* __restrict__ base, const TreeRoot* __restrict__ root, NodeArrays na,
-                             int nnodes) {
+                             const int* __restrict__ base, NodeArrays na, int nnodes, int* __restrict__ list,
+                             int* __restrict__ count) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  bool need = false;
+  if (i < n) {
+    const int lo = lp[i] + 1, d = depth[i];
+    const int k0 = base[i];
+    int par = -1;
+    if (lo > 0) {
+      const int64_t j0 = cell_begin(keys, words, n, lp, i, lo - 1);
+      par = base[j0] + (lo - 1) - (lp[j0] + 1);
+    }
+    for (int L = lo; L <= d; L++) {
+      const int k = k0 + (L - lo);
+      const int pk = L == lo ? par : k - 1;
+      na.parent[k] = pk;
+      if (pk >= 0) atomicAdd(&na.nchild[pk], 1);
+    }
+    const int k = k0 + (d - lo);
+    const int next = i + 1 < n ? base[i + 1] : nnodes;
+    na.R[k].A = make_float4(0.f, 0.f, 0.f, 0.f);
+    na.R[k].L = make_float4(0.f, 0.f, 0.f, __int_as_float(next));
+    need = d > lo;
+  }
+  warp_append(need, i, list, count);
+}
+
+__global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
+                                      const int* __restrict__ lp, const int* __restrict__ depth,
+                                      const int* __restrict__ base, const TreeRoot* __restrict__ root,
+                                      NodeArrays na, int nnodes, const int* __restrict__ list,
+                                      const int* __restrict__ count) {
   __shared__ double offs[TREE_MAX_LEVELS];  // size 2^-(L+2), exact
   const double S = root->size;
   for (int l = threadIdx.x; l < TREE_MAX_LEVELS; l += blockDim.x)
     offs[l] = dmul(S, __longlong_as_double((long long)(1023 - (l + 2)) << 52));
   __syncthreads();
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  const int lo = lp[i] + 1, d = depth[i];
-  const int k0 = base[i];
-  int par = -1;
-  if (lo > 0) {
-    const int64_t j0 = cell_begin(keys, words, n, lp, i, lo - 1);
-    par = base[j0] + (lo - 1) - (lp[j0] + 1);
-  }
-  for (int L = lo; L <= d; L++) {
-    const int k = k0 + (L - lo);
-    const int pk = L == lo ? par : k - 1;
-    na.parent[k] = pk;
-    if (pk >= 0) atomicAdd(&na.nchild[pk], 1);
-  }
-  // leaf: skip index only
-  {
-    const int k = k0 + (d - lo);
-    const int next = i + 1 < n ? base[i + 1] : nnodes;
-    na.R[k].A = make_float4(0.f, 0.f, 0.f, 0.f);
-    na.R[k].L = make_float4(0.f, 0.f, 0.f, __int_as_float(next));
-  }
-  if (d == lo) return;
-  double c[3] = {root->c[0], root->c[1], root->c[2]};
-  for (int L = 0; L < d; L++) {
-    if (L >= lo) {
-      const int k = k0 + (L - lo);
-      const int64_t end = cell_end(keys, words, n, lp, i, L);
-      const int next = end < n ? base[end] : nnodes;
-      const double size = dmul(S, __longlong_as_double((long long)(1023 - L) << 52));
-      float4 A, Lo;
-      A.x = f32_hi(c[0]);
-      A.y = f32_hi(c[1]);
-      A.z = f32_hi(c[2]);
-      A.w = (float)dmul(size, size);
-      Lo.x = f32_lo(c[0], A.x);
-      Lo.y = f32_lo(c[1], A.y);
-      Lo.z = f32_lo(c[2], A.z);
-      Lo.w = __int_as_float(next);
-      na.R[k].A = A;
-      na.R[k].L = Lo;
-      na.C[k] = make_dvec4(c[0], c[1], c[2], size);
-    }
-    if (L + 1 < d) {
-      const unsigned g = key_digit(keys, n, i, L);
-      const double off = offs[L];
+  const int cnt = *count;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+    const int64_t i = list[q];
+    const int lo = lp[i] + 1, d = depth[i];
+    const int k0 = base[i];
+    double c[3] = {root->c[0], root->c[1], root->c[2]};
+    for (int L = 0; L < d; L++) {
+      if (L >= lo) {
+        const int k = k0 + (L - lo);
+        const int64_t end = cell_end(keys, words, n, lp, i, L);
+        const int next = end < n ? base[end] : nnodes;
+        const double size = dmul(S, __longlong_as_double((long long)(1023 - L) << 52));
+        float4 A, Lo;
+        A.x = f32_hi(c[0]);
+        A.y = f32_hi(c[1]);
+        A.z = f32_hi(c[2]);
+        A.w = (float)dmul(size, size);
+        Lo.x = f32_lo(c[0], A.x);
+        Lo.y = f32_lo(c[1], A.y);
+        Lo.z = f32_lo(c[2], A.z);
+        Lo.w = __int_as_float(next);
+        na.R[k].A = A;
+        na.R[k].L = Lo;
+        na.C[k] = make_dvec4(c[0], c[1], c[2], size);
+      }
+      if (L + 1 < d) {
+        const unsigned g = key_digit(keys, n, i, L);
+        const double off = offs[L];
 #pragma unroll
-      for (int q = 0; q < 3; q++) c[q] = ((g >> q) & 1u) ? dadd(c[q], off) : dsub(c[q], off);
+        for (int r = 0; r < 3; r++) c[r] = ((g >> r) & 1u) ? dadd(c[r], off) : dsub(c[r], off);
+      }
     }
   }
 }
@@ -470,6 +519,15 @@ __device__ __forceinline__ void store_mixed_com(const NodeArrays& na, int k, dou
   const float hx = (float)x, hy = (float)y, hz = (float)z;
   na.R[k].Mh = make_float4(hx, hy, hz, (float)m);
   na.R[k].Ml = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), 0.f);
+}
+
+// 1/m from the hardware approximation and two Newton steps y <- y + y (1 - m y).
+__device__ __forceinline__ double rcp_f64(double m) {
+  double y;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(m));
+#pragma unroll
+  for (int it = 0; it < 2; it++) y = fma(y, fma(-m, y, 1.0), y);
+  return y;
 }
 
 __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ lp, const int* __restrict__ depth,
@@ -503,7 +561,11 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
       m = dadd(m, fb.y);
     }
     na.F[par] = make_dvec4(fx, fy, fz, m);
-    const double cx = ddiv(fx, m), cy = ddiv(fy, m), cz = ddiv(fz, m);
+    // firstmoment / mass (_jbgrav.c:478) as a product with a Newton-refined reciprocal:
+    // within an ulp or two of the quotient, at a third of the FP64 work of three
+    // divisions (this loop runs on few lanes of a warp)
+    const double r = rcp_f64(m);
+    const double cx = dmul(fx, r), cy = dmul(fy, r), cz = dmul(fz, r);
     na.M[par] = make_dvec4(cx, cy, cz, m);
     store_mixed_com(na, par, cx, cy, cz, m);
     cur = par;
@@ -666,6 +728,7 @@ __global__ void __launch_bounds__(TW_THREADS)
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
   Buffer nA, nC, nM, nF, parent, nchild, arrive, xh[2];
+  Buffer list;                // particle lists: key fallbacks, then cell openers
   int* host_flags = nullptr;  // pinned: tie, maxdepth, long run, nnodes
   int words = TREE_MIN_WORDS;
   int64_t full_sort_n = -1;  // particle count whose last build needed the full multi-word sort
@@ -712,7 +775,9 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.depth, n * sizeof(int)));
   GH_TRY(ensure(ws.base, (n + 1) * sizeof(int)));
   GH_TRY(ensure(ws.scan, scan_scratch_ints(n) * sizeof(int)));
-  GH_TRY(ensure(ws.flags, 4 * sizeof(int)));
+  // flags: [0] full-key tie, [1] deepest level, [2] long run, [3] key fallbacks, [4] cell openers
+  GH_TRY(ensure(ws.flags, 8 * sizeof(int)));
+  GH_TRY(ensure(ws.list, n * sizeof(int)));
   GH_TRY(ensure(ws.idx, n * sizeof(uint32_t)));
   GH_TRY(ensure(ws.idx_tmp, n * sizeof(uint32_t)));
   GH_TRY(ensure(ws.rs, radix_scratch_words(n) * sizeof(uint32_t)));
@@ -728,9 +793,13 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
     uint64_t* ktmp = (uint64_t*)ws.keys_tmp.ptr;
     uint32_t* idx = (uint32_t*)ws.idx.ptr;
     uint32_t* itmp = (uint32_t*)ws.idx_tmp.ptr;
-    keys_kernel<<<gn, T, 0, st>>>(pos, n, root, words, keys, idx);
+    int* flags = (int*)ws.flags.ptr;
+    GH_CUDA_TRY(cudaMemsetAsync(flags, 0, 8 * sizeof(int), st));
+    keys_kernel<<<gn, T, 0, st>>>(pos, n, root, words, keys, idx, (int*)ws.list.ptr, flags + 3);
     GH_LAUNCH_CHECK();
-    GH_CUDA_TRY(cudaMemsetAsync(ws.flags.ptr, 0, 4 * sizeof(int), st));
+    keys_exact_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(pos, n, root, words, keys, (const int*)ws.list.ptr,
+                                                                flags + 3);
+    GH_LAUNCH_CHECK();
     if (full_sort) {
       GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, words, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
     } else {
@@ -780,9 +849,18 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   NodeArrays na = node_arrays(ws);
   GH_CUDA_TRY(cudaMemsetAsync(ws.nchild.ptr, 0, (size_t)nnodes * sizeof(int), st));
   GH_CUDA_TRY(cudaMemsetAsync(ws.arrive.ptr, 0, (size_t)nnodes * sizeof(int), st));
-  nodes_kernel<<<gn, T, 0, st>>>((const uint64_t*)ws.keys.ptr, words, n, (const int*)ws.lp.ptr,
-                                 (const int*)ws.depth.ptr, (const int*)ws.base.ptr, root, na, nnodes);
-  GH_LAUNCH_CHECK();
+  {
+    const uint64_t* keys = (const uint64_t*)ws.keys.ptr;
+    const int* lp = (const int*)ws.lp.ptr;
+    const int* dep = (const int*)ws.depth.ptr;
+    const int* bs = (const int*)ws.base.ptr;
+    int* openers = (int*)ws.flags.ptr + 4;
+    nodes_kernel<<<gn, T, 0, st>>>(keys, words, n, lp, dep, bs, na, nnodes, (int*)ws.list.ptr, openers);
+    GH_LAUNCH_CHECK();
+    nodes_internal_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(keys, words, n, lp, dep, bs, root, na, nnodes,
+                                                                    (const int*)ws.list.ptr, openers);
+    GH_LAUNCH_CHECK();
+  }
   // 5. monopoles
   com_up_kernel<<<gn, T, 0, st>>>(na, n, (const int*)ws.lp.ptr, (const int*)ws.depth.ptr, (const int*)ws.base.ptr,
                                   (const uint32_t*)ws.idx.ptr, pos, mass);
