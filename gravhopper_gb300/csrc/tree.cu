@@ -576,6 +576,7 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
 // Walk
 // ---------------------------------------------------------------------------
 constexpr int TW_THREADS = 128;
+constexpr int TW_MINB = 10;  // 48 registers: 40 warps per SM (measured: 9 and 11+ CTAs/SM are slower)
 
 __device__ __forceinline__ double rsqrt_f64(double s) {
   double y;
@@ -596,7 +597,7 @@ __device__ __forceinline__ double rsqrt_f64(double s) {
 constexpr int TW_FOLD = 32;
 
 template <bool GUARD, bool MIXED, bool STATS, class Epi>
-__global__ void __launch_bounds__(TW_THREADS)
+__global__ void __launch_bounds__(TW_THREADS, TW_MINB)
     tree_walk_kernel(const WalkRec* __restrict__ nR, const dvec4* __restrict__ nC, const dvec4* __restrict__ nM,
                      int nnodes, const double* __restrict__ tpos, const uint32_t* __restrict__ order, int64_t nt,
                      double eps2, double theta, float th2_lo, float th2_hi, Epi epi,
