@@ -367,16 +367,19 @@ __global__ void count_kernel(const int* __restrict__ lp, int64_t n, int* __restr
 // ---------------------------------------------------------------------------
 // 4. Nodes in preorder
 // ---------------------------------------------------------------------------
-// The walk's per-node record: one 64-byte line read per visited cell.
-struct __align__(64) WalkRec {
+// The walk's per-node record, 48 bytes (two 32-byte sectors) per visited cell.  A
+// leaf's "centre" is its particle's position and its offset is zero, so the offset
+// from the target computed for the opening test is, plus O, the offset of the centre
+// of mass: accepted cells are at least size/theta away, so O's FP32 rounding is below
+// 2^-24 theta of the distance.
+struct __align__(16) WalkRec {
   float4 A;   // (cx_hi, cy_hi, cz_hi, size^2)        FP32 opening prefilter
   float4 L;   // (cx_lo, cy_lo, cz_lo, next as bits)   FP32 residuals + skip index
-  float4 Mh;  // (comx_hi, comy_hi, comz_hi, mass)     mixed-precision interaction
-  float4 Ml;  // (comx_lo, comy_lo, comz_lo, 0)
+  float4 O;   // (com - c as FP32, mass)              mixed-precision interaction
 };
 
 struct NodeArrays {
-  WalkRec* R;    // walk records (A, L, Mh, Ml)
+  WalkRec* R;    // walk records (A, L, O)
   dvec4* C;      // (cx, cy, cz, size)                    exact opening test (internal cells)
   dvec4* M;      // (comx, comy, comz, mass)              interaction
   dvec4* F;      // (first moment x, y, z, mass)          build only
@@ -513,13 +516,6 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
 // depend on which child arrives last, so the result is deterministic.
 __device__ __forceinline__ int node_next(const WalkRec* __restrict__ R, int k) { return __float_as_int(R[k].L.w); }
 
-// FP32 hi/lo split of a cell's centre of mass, for the mixed-precision walk.
-__device__ __forceinline__ void store_mixed_com(const NodeArrays& na, int k, double x, double y, double z,
-                                                double m) {
-  const float hx = (float)x, hy = (float)y, hz = (float)z;
-  na.R[k].Mh = make_float4(hx, hy, hz, (float)m);
-  na.R[k].Ml = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), 0.f);
-}
 
 // 1/m from the hardware approximation and two Newton steps y <- y + y (1 - m y).
 __device__ __forceinline__ double rcp_f64(double m) {
@@ -542,7 +538,11 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
     const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
     na.M[cur] = make_dvec4(x, y, z, m);
     na.F[cur] = make_dvec4(dmul(m, x), dmul(m, y), dmul(m, z), m);
-    store_mixed_com(na, cur, x, y, z, m);
+    // walk record: the particle's position as the leaf's centre (hi/lo), zero offset
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    na.R[cur].A = make_float4(hx, hy, hz, 0.f);
+    na.R[cur].L = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), na.R[cur].L.w);
+    na.R[cur].O = make_float4(0.f, 0.f, 0.f, (float)m);
   }
   for (;;) {
     const int par = na.parent[cur];
@@ -567,7 +567,8 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
     const double r = rcp_f64(m);
     const double cx = dmul(fx, r), cy = dmul(fy, r), cz = dmul(fz, r);
     na.M[par] = make_dvec4(cx, cy, cz, m);
-    store_mixed_com(na, par, cx, cy, cz, m);
+    const dvec4 C = na.C[par];
+    na.R[par].O = make_float4((float)dsub(cx, C.x), (float)dsub(cy, C.y), (float)dsub(cz, C.z), (float)m);
     cur = par;
   }
 }
@@ -590,9 +591,10 @@ __device__ __forceinline__ double rsqrt_f64(double s) {
   return y;
 }
 
-// MIXED: accepted cells interact in FP32 on hi/lo split coordinates (the
-// difference keeps ~2^-48 of |x|), partial sums folded into a two-sum (hi, lo)
-// accumulator every 32 interactions; otherwise FP64 with a Newton-refined rsqrt.
+// MIXED: accepted cells interact in FP32: the hi/lo split offset of the cell's
+// centre (keeps ~2^-48 of |x|) plus the FP32 offset of its centre of mass; partial
+// sums folded into a two-sum (hi, lo) accumulator every 32 interactions.  Otherwise
+// FP64 with a Newton-refined rsqrt.
 // The opening decisions are the same exact ones in both forms.
 constexpr int TW_FOLD = 32;
 
@@ -632,10 +634,10 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       const float4 Lo = nR[node].L;
       const int nx = __float_as_int(Lo.w);
       bool accept = (nx == node + 1);  // leaf
+      const float dx = (A.x - h0) + (Lo.x - l0);
+      const float dy = (A.y - h1) + (Lo.y - l1);
+      const float dz = (A.z - h2) + (Lo.z - l2);
       if (!accept) {
-        const float dx = (A.x - h0) + (Lo.x - l0);
-        const float dy = (A.y - h1) + (Lo.y - l1);
-        const float dz = (A.z - h2) + (Lo.z - l2);
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float s2 = A.w;
         const bool usable = d2 > near2 && d2 > 1e-30f && d2 < 1e30f && s2 > 1e-30f;
@@ -657,18 +659,15 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       if (accept) {
         if (STATS) n_inter++;
         if (MIXED) {
-          const float4 H = nR[node].Mh;
-          const float4 Q = nR[node].Ml;
-          const float dx = (H.x - h0) + (Q.x - l0);
-          const float dy = (H.y - h1) + (Q.y - l1);
-          const float dz = (H.z - h2) + (Q.z - l2);
-          const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, eps2f)));
+          const float4 O = nR[node].O;
+          const float ex = dx + O.x, ey = dy + O.y, ez = dz + O.z;
+          const float s = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2f)));
           float r = rsqrt_approx(s);
           if (GUARD) r = s > 0.f ? r : 0.f;
-          const float f = H.w * (r * (r * r));
-          px = fmaf(f, dx, px);
-          py = fmaf(f, dy, py);
-          pz = fmaf(f, dz, pz);
+          const float f = O.w * (r * (r * r));
+          px = fmaf(f, ex, px);
+          py = fmaf(f, ey, py);
+          pz = fmaf(f, ez, pz);
           if (++pending == TW_FOLD) {
             float sx, ex;
             two_sum(hx, px, sx, ex);
