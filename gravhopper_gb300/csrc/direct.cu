@@ -111,7 +111,7 @@ static int auto_shape(int64_t np, int64_t nt) {
   return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
 }
 
-template <bool G, int T, int P, int B, class Epi, int PK = 1>
+template <bool G, int T, int P, int B, class Epi, bool PK = true>
 static int launch_shape(const StreamK& sk, const float4* src, int64_t np, const float4* tgt, int64_t nt,
                         float eps2, float* partials, int* counters, const Epi& epi, cudaStream_t st) {
   direct_mixed_kernel<G, T, P, B, Epi, PK><<<(unsigned)sk.grid, T, 0, st>>>(src, np, tgt, nt, eps2, sk, partials,
@@ -119,7 +119,7 @@ static int launch_shape(const StreamK& sk, const float4* src, int64_t np, const 
   return GH_OK;
 }
 
-template <bool G, int T, int P, int B, int PK = 1>
+template <bool G, int T, int P, int B, bool PK = true>
 static int occupancy_shape() {
   int o = 0;
   if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, direct_mixed_kernel<G, T, P, B, EpiStore, PK>, T, 0) !=
@@ -143,14 +143,10 @@ static int dispatch_shape(int shape, const StreamK& sk, const float4* src, int64
     case 6: return launch_shape<G, 128, 2, 6>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 7: return launch_shape<G, 256, 1, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
     case 8: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 9: return launch_shape<G, 256, 2, 2, Epi, 0>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 10: return launch_shape<G, 512, 2, 1, Epi, 0>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 11: return launch_shape<G, 256, 4, 1, Epi, 0>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 12: return launch_shape<G, 384, 3, 1, Epi, 0>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 13: return launch_shape<G, 384, 3, 1, Epi, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 14: return launch_shape<G, 256, 4, 1, Epi, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 15: return launch_shape<G, 256, 2, 2, Epi, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    default: return launch_shape<G, 512, 2, 1, Epi, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 9: return launch_shape<G, 256, 2, 2, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 10: return launch_shape<G, 512, 2, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 11: return launch_shape<G, 256, 4, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    default: return launch_shape<G, 384, 3, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
   }
 }
 
@@ -168,14 +164,16 @@ static int mixed_grid_cap(int num_sms, int shape, bool guard) {
       case 6: o = guard ? occupancy_shape<true, 128, 2, 6>() : occupancy_shape<false, 128, 2, 6>(); break;
       case 7: o = guard ? occupancy_shape<true, 256, 1, 4>() : occupancy_shape<false, 256, 1, 4>(); break;
       case 8: o = guard ? occupancy_shape<true, 512, 2, 2>() : occupancy_shape<false, 512, 2, 2>(); break;
-      case 9: o = guard ? occupancy_shape<true, 256, 2, 2, 0>() : occupancy_shape<false, 256, 2, 2, 0>(); break;
-      case 10: o = guard ? occupancy_shape<true, 512, 2, 1, 0>() : occupancy_shape<false, 512, 2, 1, 0>(); break;
-      case 11: o = guard ? occupancy_shape<true, 256, 4, 1, 0>() : occupancy_shape<false, 256, 4, 1, 0>(); break;
-      case 12: o = guard ? occupancy_shape<true, 384, 3, 1, 0>() : occupancy_shape<false, 384, 3, 1, 0>(); break;
-      case 13: o = guard ? occupancy_shape<true, 384, 3, 1, 2>() : occupancy_shape<false, 384, 3, 1, 2>(); break;
-      case 14: o = guard ? occupancy_shape<true, 256, 4, 1, 2>() : occupancy_shape<false, 256, 4, 1, 2>(); break;
-      case 15: o = guard ? occupancy_shape<true, 256, 2, 2, 2>() : occupancy_shape<false, 256, 2, 2, 2>(); break;
-      default: o = guard ? occupancy_shape<true, 512, 2, 1, 2>() : occupancy_shape<false, 512, 2, 1, 2>(); break;
+      case 9: o = guard ? occupancy_shape<true, 256, 2, 2, false>() : occupancy_shape<false, 256, 2, 2, false>(); break;
+      case 10:
+        o = guard ? occupancy_shape<true, 512, 2, 1, false>() : occupancy_shape<false, 512, 2, 1, false>();
+        break;
+      case 11:
+        o = guard ? occupancy_shape<true, 256, 4, 1, false>() : occupancy_shape<false, 256, 4, 1, false>();
+        break;
+      default:
+        o = guard ? occupancy_shape<true, 384, 3, 1, false>() : occupancy_shape<false, 384, 3, 1, false>();
+        break;
     }
   }
   return o * num_sms;

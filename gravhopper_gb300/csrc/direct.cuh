@@ -271,10 +271,8 @@ struct MixedShape {
 };
 constexpr MixedShape kMixedShapes[] = {{256, 2, 2}, {256, 4, 1}, {128, 4, 2}, {128, 2, 4}, {512, 2, 1},
                                        {256, 2, 3}, {128, 2, 6}, {256, 1, 4}, {512, 2, 2},
-                                       {256, 2, 2}, {512, 2, 1}, {256, 4, 1}, {384, 3, 1},
-                                       {384, 3, 1}, {256, 4, 1}, {256, 2, 2}, {512, 2, 1}};
-// Shapes 0-8 run the packed f32x2 loop (mixed_chunk), 9-12 the scalar FP32 loop
-// (mixed_chunk_scalar), 13-16 the hybrid loop (mixed_chunk_hybrid).
+                                       {256, 2, 2}, {512, 2, 1}, {256, 4, 1}, {384, 3, 1}};
+// Shapes 9-12 run the scalar FP32 loop (mixed_chunk_scalar); 0-8 the packed f32x2 loop.
 constexpr int kNumMixedShapes = (int)(sizeof(kMixedShapes) / sizeof(kMixedShapes[0]));
 
 struct StreamK {
@@ -396,74 +394,13 @@ __device__ __forceinline__ void mixed_chunk_scalar(const float4* __restrict__ ti
   }
 }
 
-// Hybrid chunk: the offsets and r^2 of two targets per f32x2 instruction (doubled
-// source layout, as mixed_chunk), then the rsqrt results' tail in scalar FP32, so
-// that no MUFU result has to be moved into a register pair: per two pairs 6 packed
-// + 12 scalar FMA-pipe instructions and 2 MUFU, against 24 + 2 for the scalar loop.
-template <bool GUARD, int P, int JT>
-__device__ __forceinline__ void mixed_chunk_hybrid(const float4* __restrict__ tile, const f2* tx, const f2* ty,
-                                                   const f2* tz, f2 E2, f2* hx, f2* hy, f2* hz, f2* lx, f2* ly,
-                                                   f2* lz) {
-  constexpr int R = 2 * P;
-  float ax[R], ay[R], az[R];
-#pragma unroll
-  for (int r = 0; r < R; r++) ax[r] = ay[r] = az[r] = 0.f;
-#pragma unroll 4
-  for (int k = 0; k < JT; k++) {
-    const float4 a = tile[2 * k + 0];
-    const float4 b = tile[2 * k + 1];
-    const f2 X = f2make(a.x, a.y), Y = f2make(a.z, a.w), Z = f2make(b.x, b.y);
-    const float m = b.z;
-#pragma unroll
-    for (int p = 0; p < P; p++) {
-      const f2 dx = f2sub(X, tx[p]);
-      const f2 dy = f2sub(Y, ty[p]);
-      const f2 dz = f2sub(Z, tz[p]);
-      f2 r2 = f2fma(dx, dx, E2);
-      r2 = f2fma(dy, dy, r2);
-      r2 = f2fma(dz, dz, r2);
-      float r2a, r2b, dxa, dxb, dya, dyb, dza, dzb;
-      f2split(r2, r2a, r2b);
-      f2split(dx, dxa, dxb);
-      f2split(dy, dya, dyb);
-      f2split(dz, dza, dzb);
-      float ia = rsqrt_approx(r2a), ib = rsqrt_approx(r2b);
-      if (GUARD) {
-        ia = r2a > 0.f ? ia : 0.f;
-        ib = r2b > 0.f ? ib : 0.f;
-      }
-      const float sa = (m * ia) * (ia * ia), sb = (m * ib) * (ib * ib);
-      ax[2 * p] = fmaf(sa, dxa, ax[2 * p]);
-      ay[2 * p] = fmaf(sa, dya, ay[2 * p]);
-      az[2 * p] = fmaf(sa, dza, az[2 * p]);
-      ax[2 * p + 1] = fmaf(sb, dxb, ax[2 * p + 1]);
-      ay[2 * p + 1] = fmaf(sb, dyb, ay[2 * p + 1]);
-      az[2 * p + 1] = fmaf(sb, dzb, az[2 * p + 1]);
-    }
-  }
-#pragma unroll
-  for (int p = 0; p < P; p++) {
-    f2 s, e;
-    f2two_sum(hx[p], f2make(ax[2 * p], ax[2 * p + 1]), s, e);
-    hx[p] = s;
-    lx[p] = f2add(lx[p], e);
-    f2two_sum(hy[p], f2make(ay[2 * p], ay[2 * p + 1]), s, e);
-    hy[p] = s;
-    ly[p] = f2add(ly[p], e);
-    f2two_sum(hz[p], f2make(az[2 * p], az[2 * p + 1]), s, e);
-    hz[p] = s;
-    lz[p] = f2add(lz[p], e);
-  }
-}
-
 // Per-CTA scratch for split tiles: 2 slots (first and last tile of its range),
 // each 6 floats (hi/lo for x, y, z) per target of a tile.
 __host__ __device__ constexpr int64_t mixed_slot_floats(int threads, int packs) {
   return (int64_t)6 * threads * 2 * packs;
 }
 
-// MODE: 1 packed f32x2 loop, 0 scalar loop, 2 hybrid loop.
-template <bool GUARD, int THREADS, int P, int MINB, class Epi, int MODE = 1>
+template <bool GUARD, int THREADS, int P, int MINB, class Epi, bool PACKED = true>
 __global__ void __launch_bounds__(THREADS, MINB)
     direct_mixed_kernel(const float4* __restrict__ src, int64_t np, const float4* __restrict__ tgt,
                         int64_t nt, float eps2, StreamK sk, float* __restrict__ partials,
@@ -515,7 +452,7 @@ __global__ void __launch_bounds__(THREADS, MINB)
     }
     for (int64_t c = c0; c < c1; c++) {
       float4* tb = tile + buf * (2 * JT);
-      if (MODE != 0) {
+      if (PACKED) {
         tb[2 * tid + 0] = make_float4(pre.x, pre.x, pre.y, pre.y);
         tb[2 * tid + 1] = make_float4(pre.z, pre.z, pre.w, pre.w);
       } else {
@@ -526,10 +463,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
         const int64_t j = (c + 1) * JT + tid;
         pre = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
       }
-      if (MODE == 1)
+      if (PACKED)
         mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
-      else if (MODE == 2)
-        mixed_chunk_hybrid<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
       else
         mixed_chunk_scalar<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
       buf ^= 1;
