@@ -24,6 +24,7 @@ def main(argv=None):
     ap.add_argument("--theta", type=float, default=0.7)
     ap.add_argument("--systems", type=int, default=64)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"], help="tree and vjp cases")
+    ap.add_argument("--shape", type=int, default=-1, help="direct: mixed kernel tile shape (-1 auto)")
     ap.add_argument("--fp64-form", type=int, default=-1, choices=[-1, 0, 1],
                     help="direct64: FP64 kernel (0 thread per target, 1 ordered CTA-wide terms, -1 auto)")
     a = ap.parse_args(argv)
@@ -34,6 +35,7 @@ def main(argv=None):
     dev = torch.device("cuda", 0)
     _capi.load()
     _capi.call("gh_direct_set_fp64_form", a.fp64_form)
+    _capi.call("gh_direct_set_shape", a.shape)
     if a.case in ("direct", "direct64", "vjp"):
         ic = ics.plummer(a.n, seed=0)
     elif a.case == "tree":

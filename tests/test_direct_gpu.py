@@ -139,3 +139,23 @@ def test_fp64_forms_bit_exact(lib, cuda, form):
                 oracle.direct_summation_position(ic["pos"], ic["mass"], fp[:nt], 5e-5))
     finally:
         _capi.call("gh_direct_set_fp64_form", -1)
+
+
+def test_every_mixed_shape(lib, cuda):
+    """Every compiled tile shape of the mixed kernel (packed and scalar loops) meets the
+    mixed tolerance, for self forces and target points."""
+    from gravhopper_gb300 import _capi, _jbgrav, ics
+    ic = ics.plummer(5000, seed=13)
+    rng = np.random.default_rng(3)
+    fp = rng.normal(size=(777, 3)) * 2e-3
+    ref = oracle.direct_summation(ic["pos"], ic["mass"], 5e-5)
+    ref_p = oracle.direct_summation_position(ic["pos"], ic["mass"], fp, 5e-5)
+    try:
+        for shape in range(int(_capi.load().gh_direct_num_shapes())):
+            _capi.call("gh_direct_set_shape", shape)
+            rms, mx = rel_err(_jbgrav.direct_summation_mixed(ic["pos"], ic["mass"], 5e-5), ref)
+            assert rms <= 1e-6 and mx <= 1e-3, (shape, rms, mx)
+            rms, mx = rel_err(_jbgrav.direct_summation_mixed(ic["pos"], ic["mass"], 5e-5, force_pos=fp), ref_p)
+            assert rms <= 1e-6 and mx <= 1e-3, (shape, rms, mx)
+    finally:
+        _capi.call("gh_direct_set_shape", -1)
