@@ -380,7 +380,7 @@ def measure_tree(dev, n=1 << 20, steps=2):
             engine.run_dkd(x, v, m, 1, 0.5, 0.1, algorithm="tree", theta=theta, precision=prec)
             _capi.tree_stats(False)
             c = _capi.tree_stats_read()
-            rec_bytes = 64 * c["cell_steps"]
+            rec_bytes = 48 * c["cell_steps"]  # one 48-byte cell record per warp step
             out[key][prec] = {"particle_steps_per_s": n * steps / t, "ms_per_step": t / steps * 1e3,
                               "walk_ms_per_step": walk_s * 1e3,
                               "build_ms_per_step": t / steps * 1e3 - walk_s * 1e3,
@@ -391,7 +391,7 @@ def measure_tree(dev, n=1 << 20, steps=2):
                               "record_bytes_per_walk": rec_bytes,
                               "record_read_gbs": rec_bytes / walk_s / 1e9,
                               "record_read_frac_of_measured_l2": rec_bytes / walk_s / l2,
-                              "per_target_record_gbs": 64 * c["target_visits"] / walk_s / 1e9}
+                              "per_target_record_gbs": 48 * c["target_visits"] / walk_s / 1e9}
     # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
     # its serial build plus the threaded walk of 16384 targets scaled to all N targets
     # (the faster of two calls).

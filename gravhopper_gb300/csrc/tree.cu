@@ -30,6 +30,7 @@
 // recomputed with the reference's FP64 operations, so every lane takes exactly the
 // reference's decisions.  Accepted cells contribute (COM - x) m / (r^2 + eps^2)^1.5 in
 // FP64, with the reference's zero for r^2 + eps^2 == 0 (_jbgrav.c:514-520).
+#include <cmath>
 #include <mutex>
 
 #include "direct.cuh"
@@ -577,7 +578,7 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
 // Walk
 // ---------------------------------------------------------------------------
 constexpr int TW_THREADS = 128;
-constexpr int TW_MINB = 10;  // 48 registers: 40 warps per SM (measured: 9 and 11+ CTAs/SM are slower)
+constexpr int TW_MINB = 9;  // 56 registers, no spills: 36 warps per SM (measured fastest)
 
 __device__ __forceinline__ double rsqrt_f64(double s) {
   double y;
@@ -615,8 +616,10 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
   }
   const float h0 = (float)p0, h1 = (float)p1, h2 = (float)p2;
   const float l0 = f32_lo(p0, h0), l1 = f32_lo(p1, h1), l2 = f32_lo(p2, h2);
-  // d^2 below this needs the exact test: FP32 differences lose too much relative to |x|
-  const float near2 = 1e-18f * (h0 * h0 + h1 * h1 + h2 * h2);
+  // d^2 below this needs the exact test: FP32 differences lose too much relative to
+  // |x|, and FP32 stays in its normal range (with theta >= 1e-3 a cell whose size^2
+  // is below that range is then accepted, as the exact test would)
+  const float near2 = fmaxf(1e-18f * (h0 * h0 + h1 * h1 + h2 * h2), 1e-30f);
   const float eps2f = (float)eps2;
   double ax = 0.0, ay = 0.0, az = 0.0;
   float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
@@ -632,6 +635,8 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       if (STATS) n_visit++;
       const float4 A = nR[node].A;
       const float4 Lo = nR[node].L;
+      float4 O;  // loaded with the rest of the record: most visits are accepted
+      if (MIXED) O = nR[node].O;
       const int nx = __float_as_int(Lo.w);
       bool accept = (nx == node + 1);  // leaf
       const float dx = (A.x - h0) + (Lo.x - l0);
@@ -640,7 +645,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       if (!accept) {
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float s2 = A.w;
-        const bool usable = d2 > near2 && d2 > 1e-30f && d2 < 1e30f && s2 > 1e-30f;
+        const bool usable = d2 > near2 && d2 < 1e30f;
         if (usable && s2 < th2_lo * d2) {
           accept = true;
         } else if (usable && s2 > th2_hi * d2) {
@@ -659,7 +664,6 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       if (accept) {
         if (STATS) n_inter++;
         if (MIXED) {
-          const float4 O = nR[node].O;
           const float ex = dx + O.x, ey = dy + O.y, ez = dz + O.z;
           const float s = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2f)));
           float r = rsqrt_approx(s);
@@ -895,10 +899,14 @@ static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const 
                      double eps, double theta, int precision, const Epi& epi, cudaStream_t st) {
   if (nt == 0) return GH_OK;
   const double eps2 = eps * eps;
-  float lo = -1.f, hi = -1.f;  // theta <= 0 or NaN: never open by the prefilter, never accept
-  if (theta > 0.0) {
+  // theta <= 0 or NaN: the prefilter opens every cell and accepts none; below 1e-3
+  // it decides nothing (every internal cell takes the exact test)
+  float lo = -1.f, hi = -1.f;
+  if (theta >= 1e-3) {
     lo = (float)(theta * theta * (1.0 - TREE_MARGIN));
     hi = (float)(theta * theta * (1.0 + TREE_MARGIN));
+  } else if (theta > 0.0) {
+    hi = INFINITY;
   }
   NodeArrays na = node_arrays(ws);
   const bool mixed = precision == GH_PREC_MIXED;
