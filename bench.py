@@ -387,6 +387,7 @@ def measure_tree(dev, n=1 << 20, steps=2):
                               "interactions_per_target": c["interactions"] / n,
                               "cells_visited_per_target": c["target_visits"] / n,
                               "exact_tests_per_target": c["exact_tests"] / n,
+                              "leaf_interactions_per_target": c["leaf_interactions"] / n,
                               "warp_cell_steps": c["cell_steps"],
                               "record_bytes_per_walk": rec_bytes,
                               "record_read_gbs": rec_bytes / walk_s / 1e9,

@@ -176,9 +176,10 @@ def tree_stats(enable: bool) -> None:
 
 
 def tree_stats_read():
-    """Counters since the last read: walks, warp cell steps (64-byte records read),
-    cells visited summed over targets, target-cell interactions, exact FP64 opening tests."""
-    out = (ctypes.c_int64 * 5)()
+    """Counters since the last read: walks, warp cell steps (48-byte records read),
+    cells visited summed over targets, target-cell interactions, exact FP64 opening
+    tests, interactions with leaves."""
+    out = (ctypes.c_int64 * 6)()
     call("gh_tree_stats_read", ctypes.addressof(out))
     return {"walks": out[0], "cell_steps": out[1], "target_visits": out[2], "interactions": out[3],
-            "exact_tests": out[4]}
+            "exact_tests": out[4], "leaf_interactions": out[5]}

@@ -625,7 +625,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
   float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
   float hx = 0.f, hy = 0.f, hz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;  // two-sum hi, lo
   int pending = 0;
-  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0;  // walk counters (STATS)
+  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0, n_leaf = 0;  // walk counters (STATS)
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
   while (node < nnodes) {
@@ -662,7 +662,10 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
         }
       }
       if (accept) {
-        if (STATS) n_inter++;
+        if (STATS) {
+          n_inter++;
+          if (nx == node + 1) n_leaf++;
+        }
         if (MIXED) {
           const float ex = dx + O.x, ey = dy + O.y, ez = dz + O.z;
           const float s = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2f)));
@@ -711,11 +714,13 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
     n_visit = __reduce_add_sync(0xffffffffu, n_visit);
     n_inter = __reduce_add_sync(0xffffffffu, n_inter);
     n_exact = __reduce_add_sync(0xffffffffu, n_exact);
+    n_leaf = __reduce_add_sync(0xffffffffu, n_leaf);
     if ((threadIdx.x & 31) == 0) {
       atomicAdd(&stats[0], (unsigned long long)n_step);
       atomicAdd(&stats[1], (unsigned long long)n_visit);
       atomicAdd(&stats[2], (unsigned long long)n_inter);
       atomicAdd(&stats[3], (unsigned long long)n_exact);
+      atomicAdd(&stats[4], (unsigned long long)n_leaf);
     }
   }
   if (MIXED) {
@@ -874,9 +879,9 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   return GH_OK;
 }
 
-// Walk counters, off unless gh_tree_stats(1): [0] warp cell steps (one 64-byte
+// Walk counters, off unless gh_tree_stats(1): [0] warp cell steps (one 48-byte
 // record read each), [1] cells visited summed over targets, [2] target-cell
-// interactions, [3] exact FP64 opening tests.
+// interactions, [3] exact FP64 opening tests, [4] interactions with leaves.
 static bool g_stats_on = false;
 static int64_t g_stats_walks = 0;
 static Buffer g_stats[64];
@@ -917,8 +922,8 @@ static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const 
     GH_TRY(device_info(&di));
     Buffer& b = g_stats[di.device];
     if (!b.ptr) {
-      GH_TRY(ensure(b, 4 * sizeof(unsigned long long)));
-      GH_CUDA_TRY(cudaMemsetAsync(b.ptr, 0, 4 * sizeof(unsigned long long), st));
+      GH_TRY(ensure(b, 8 * sizeof(unsigned long long)));
+      GH_CUDA_TRY(cudaMemsetAsync(b.ptr, 0, 8 * sizeof(unsigned long long), st));
     }
     stats = (unsigned long long*)b.ptr;
     g_stats_walks++;
@@ -1021,7 +1026,7 @@ extern "C" int gh_tree_stats_read(int64_t* out) {
   DeviceInfo di;
   GH_TRY(device_info(&di));
   Buffer& b = g_stats[di.device];
-  unsigned long long h[4] = {0, 0, 0, 0};
+  unsigned long long h[5] = {0, 0, 0, 0, 0};
   if (b.ptr) {
     GH_CUDA_TRY(cudaDeviceSynchronize());
     GH_CUDA_TRY(cudaMemcpy(h, b.ptr, sizeof(h), cudaMemcpyDeviceToHost));
@@ -1029,7 +1034,7 @@ extern "C" int gh_tree_stats_read(int64_t* out) {
     GH_CUDA_TRY(cudaDeviceSynchronize());
   }
   out[0] = g_stats_walks;
-  for (int k = 0; k < 4; k++) out[k + 1] = (int64_t)h[k];
+  for (int k = 0; k < 5; k++) out[k + 1] = (int64_t)h[k];
   g_stats_walks = 0;
   return GH_OK;
 }

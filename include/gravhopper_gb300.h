@@ -191,14 +191,15 @@ int gh_measure_l2_read(double* bytes_per_s, void* stream);
 
 /* Enables (1) or disables (0) the tree-walk counters (no counterpart in the
  * reference, which counts nothing).  While enabled every walk adds, over its warps,
- * the cell steps (one 64-byte cell record read per warp step), the cells visited by
- * each target (what a per-target walk would read), the target-cell interactions and
- * the exact FP64 opening tests. */
+ * the cell steps (one 48-byte cell record read per warp step), the cells visited by
+ * each target (what a per-target walk would read), the target-cell interactions, the
+ * exact FP64 opening tests and the interactions with leaves. */
 int gh_tree_stats(int enable);
 
 /* Synchronises the device and returns the counters accumulated since the last read,
- * then clears them: out[0] walks, out[1] warp cell steps, out[2] target cell visits,
- * out[3] interactions, out[4] exact opening tests. */
+ * then clears them (out holds 6 entries): out[0] walks, out[1] warp cell steps,
+ * out[2] target cell visits, out[3] interactions, out[4] exact opening tests,
+ * out[5] interactions with leaves. */
 int gh_tree_stats_read(int64_t* out);
 
 #ifdef __cplusplus
