@@ -106,7 +106,7 @@ static int g_f64_form = -1;  // -1 by target count, 0 thread per target, 1 order
 // want small tiles (more CTAs share the sources), large ones the widest CTAs.
 static int auto_shape(int64_t np, int64_t nt) {
   const int64_t n = np > nt ? np : nt;
-  if (n >= (1 << 19)) return 12;  // 384 threads, 6 targets per thread, scalar FP32 loop
+  if (n >= (1 << 19)) return 10;  // 512 threads, 4 targets per thread, scalar FP32 loop
   if (n >= 8192) return 3;       // 128 threads, 2 packs, 4 CTAs/SM
   return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
 }
