@@ -1,11 +1,10 @@
 // Stable LSD radix sort (8-bit digits, multi-word keys) and exclusive scan.
 //
-// Each sort pass is three launches: per-tile digit histograms, one exclusive scan
-// of the digit-major histogram table (giving every tile its output offset per
-// digit), and a stable scatter.  Stability inside a tile comes from processing the
-// tile in rounds of one item per thread (item order = round, then thread) and
-// ranking equal digits within a warp with __match_any_sync, across warps with a
-// per-round prefix over the warp counts.
+// Each sort pass is one launch (one-sweep, below) after one histogram launch per
+// key word.  Stability inside a tile comes from processing the tile in rounds of one
+// item per thread (item order = round, then thread) and ranking equal digits within a
+// warp with __match_any_sync, across warps with a per-round prefix over the warp
+// counts; across tiles from the tiles' ticket order.
 #include "sort.cuh"
 
 namespace gh {
@@ -45,43 +44,123 @@ __device__ __forceinline__ int64_t block_exclusive_scan_1024(int64_t v, int64_t*
   return pre;
 }
 
+// ---------------------------------------------------------------------------
+// One-sweep LSD passes.  The digit histograms of every pass are counted up front
+// (they do not depend on the order of the keys); each pass is then one launch in
+// which a CTA takes the next tile by ticket, counts its tile's digits, publishes them
+// and finds its output offsets by looking back over the earlier tiles' published
+// counts (decoupled look-back).  A CTA only ever waits on tiles with smaller tickets,
+// which are already running, and every wait is bounded (OS_MAX_SPINS, then the error
+// flag is set and the sort's result is garbage).
+// ---------------------------------------------------------------------------
+constexpr uint32_t OS_AGG = 1u << 30;    // status word: tile count published
+constexpr uint32_t OS_INC = 2u << 30;    // status word: inclusive prefix published
+constexpr uint32_t OS_VAL = (1u << 30) - 1;
+constexpr int OS_MAX_SPINS = 1 << 24;
+constexpr int OS_MAX_PASSES = 8;        // 8-bit digits of one 64-bit word
+
+__device__ __forceinline__ uint32_t ld_status(const uint32_t* p) { return *(const volatile uint32_t*)p; }
+__device__ __forceinline__ void st_status(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
+
+// Digit counts of every pass of one key word: out[p*256 + d].
 __global__ void __launch_bounds__(RS_THREADS)
-    rs_hist_kernel(const uint64_t* __restrict__ kw, int64_t n, int shift, uint32_t* __restrict__ hist,
-                   int nb) {
-  __shared__ uint32_t cnt[RS_BINS];
-  cnt[threadIdx.x] = 0;
+    os_hist_kernel(const uint64_t* __restrict__ kw, int64_t n, int passes, uint32_t* __restrict__ out) {
+  __shared__ uint32_t h[OS_MAX_PASSES][RS_BINS];
+  for (int p = 0; p < OS_MAX_PASSES; p++) h[p][threadIdx.x] = 0;
   __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * RS_TILE;
-#pragma unroll
-  for (int r = 0; r < RS_ROUNDS; r++) {
-    int64_t i = base + r * RS_THREADS + threadIdx.x;
-    if (i < n) atomicAdd(&cnt[(kw[i] >> shift) & 255u], 1u);
+  for (int64_t i = (int64_t)blockIdx.x * RS_THREADS + threadIdx.x; i < n; i += (int64_t)gridDim.x * RS_THREADS) {
+    const uint64_t k = kw[i];
+    for (int p = 0; p < passes; p++) atomicAdd(&h[p][(k >> (8 * p)) & 255u], 1u);
   }
   __syncthreads();
-  hist[(int64_t)threadIdx.x * nb + blockIdx.x] = cnt[threadIdx.x];
+  for (int p = 0; p < passes; p++)
+    if (h[p][threadIdx.x]) atomicAdd(&out[p * RS_BINS + threadIdx.x], h[p][threadIdx.x]);
+}
+
+// Counts -> exclusive digit offsets, for `np` passes of 256 digits each, in place.
+__global__ void __launch_bounds__(RS_BINS) os_offsets_kernel(uint32_t* __restrict__ off, int np) {
+  __shared__ uint32_t ws[RS_BINS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int q = 0; q < np; q++) {
+    const uint32_t v = off[q * RS_BINS + threadIdx.x];
+    uint32_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (lane == 31) ws[warp] = x;
+    __syncthreads();
+    uint32_t before = 0;
+    for (int k = 0; k < warp; k++) before += ws[k];
+    off[q * RS_BINS + threadIdx.x] = before + x - v;
+    __syncthreads();
+  }
 }
 
 __global__ void __launch_bounds__(RS_THREADS)
-    rs_scatter_kernel(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ iin,
-                      uint64_t* __restrict__ kout, uint32_t* __restrict__ iout, int words, int64_t n,
-                      int w, int shift, const uint32_t* __restrict__ hist, int nb) {
+    os_pass_kernel(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ iin, uint64_t* __restrict__ kout,
+                   uint32_t* __restrict__ iout, int words, int64_t n, int w, int shift,
+                   const uint32_t* __restrict__ doff, uint32_t* __restrict__ status, int* __restrict__ ticket,
+                   int* __restrict__ err) {
   constexpr int NW = RS_THREADS / 32;
   __shared__ uint32_t warp_cnt[NW][RS_BINS];
   __shared__ uint32_t warp_off[NW][RS_BINS];
   __shared__ uint32_t cursor[RS_BINS];
   __shared__ uint32_t round_tot[RS_BINS];
+  __shared__ uint32_t tile_cnt[RS_BINS];
+  __shared__ int s_tile;
   static_assert(RS_THREADS == RS_BINS, "one digit bin per thread");
   const int tid = threadIdx.x, warp = tid >> 5;
+  if (tid == 0) s_tile = atomicAdd(ticket, 1);
+  tile_cnt[tid] = 0;
 #pragma unroll
   for (int k = 0; k < NW; k++) warp_cnt[k][tid] = 0;
-  cursor[tid] = hist[(int64_t)tid * nb + blockIdx.x];
   __syncthreads();
-  const int64_t base = (int64_t)blockIdx.x * RS_TILE;
+  const int tile = s_tile;
+  const int64_t base = (int64_t)tile * RS_TILE;
   const uint64_t* kw = kin + (int64_t)w * n;
+  unsigned dig[RS_ROUNDS];
+#pragma unroll
+  for (int r = 0; r < RS_ROUNDS; r++) {
+    const int64_t i = base + r * RS_THREADS + tid;
+    dig[r] = i < n ? (unsigned)((kw[i] >> shift) & 255u) : 256u;
+    const unsigned peers = __match_any_sync(0xffffffffu, dig[r]);
+    if (dig[r] < 256u && (peers & lanemask_lt()) == 0) atomicAdd(&tile_cnt[dig[r]], (uint32_t)__popc(peers));
+  }
+  __syncthreads();
+  // publish this tile's count of digit tid, then add up the earlier tiles' counts
+  const uint32_t cnt = tile_cnt[tid];
+  uint32_t excl = 0;
+  uint32_t* my = status + (int64_t)tile * RS_BINS + tid;
+  if (tile == 0) {
+    st_status(my, OS_INC | cnt);
+  } else {
+    st_status(my, OS_AGG | cnt);
+    for (int t = tile - 1; t >= 0; t--) {
+      const uint32_t* ps = status + (int64_t)t * RS_BINS + tid;
+      uint32_t v = ld_status(ps);
+      for (int spin = 0; (v >> 30) == 0; spin++) {
+        if (spin >= OS_MAX_SPINS) {
+          atomicOr(err, 1);
+          v = OS_INC;
+          break;
+        }
+        v = ld_status(ps);
+      }
+      excl += v & OS_VAL;
+      if ((v & ~OS_VAL) == OS_INC) break;
+    }
+    st_status(my, OS_INC | (excl + cnt));
+  }
+  cursor[tid] = doff[tid] + excl;
+  __syncthreads();
+  // stable ranks in item order: rounds of one item per thread, warps in order
+#pragma unroll
   for (int r = 0; r < RS_ROUNDS; r++) {
     const int64_t i = base + r * RS_THREADS + tid;
     const bool valid = i < n;
-    const unsigned d = valid ? (unsigned)((kw[i] >> shift) & 255u) : 256u;
+    const unsigned d = dig[r];
     const unsigned peers = __match_any_sync(0xffffffffu, d);
     const unsigned rank = __popc(peers & lanemask_lt());
     if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
@@ -90,7 +169,7 @@ __global__ void __launch_bounds__(RS_THREADS)
       uint32_t run = 0;
 #pragma unroll
       for (int k = 0; k < NW; k++) {
-        uint32_t c = warp_cnt[k][tid];
+        const uint32_t c = warp_cnt[k][tid];
         warp_off[k][tid] = run;
         run += c;
         warp_cnt[k][tid] = 0;
@@ -109,40 +188,52 @@ __global__ void __launch_bounds__(RS_THREADS)
   }
 }
 
-// Scratch layout: the digit-major histogram table (RS_BINS * nb + 1 entries, scanned
-// in place) followed by the multi-block scan's tile sums.
+// Scratch layout (u32 words): digit offsets of every pass (passes * 256), tile status
+// words of every pass (passes * tiles * 256), one ticket per pass, the error flag.
+static int64_t os_tiles(int64_t n) { return (n + RS_TILE - 1) / RS_TILE; }
+
 int64_t radix_scratch_words(int64_t n) {
-  const int64_t nb = (n + RS_TILE - 1) / RS_TILE;
-  const int64_t m = (int64_t)RS_BINS * (nb > 0 ? nb : 1);
-  return m + 1 + scan_scratch_ints(m);
+  const int64_t passes = (int64_t)6 * OS_MAX_PASSES;  // up to six key words
+  const int64_t tiles = os_tiles(n) > 0 ? os_tiles(n) : 1;
+  return passes * RS_BINS + passes * tiles * RS_BINS + passes + 1;
 }
 
 int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t* idx_tmp, int words,
-                    int bits_per_word, int64_t n, uint32_t* scratch_u32, cudaStream_t st) {
+                    int bits_per_word, int64_t n, uint32_t* scratch_u32, cudaStream_t st, int* err) {
   if (n <= 1) return GH_OK;
-  const int nb = (int)((n + RS_TILE - 1) / RS_TILE);
+  if (words < 1 || words > 6) return set_error(GH_ERR_ARG, "radix sort: %d key words", words);
+  const int64_t tiles = os_tiles(n);
   const int passes = (bits_per_word + 7) / 8;
+  const int np = words * passes;
+  uint32_t* doff = scratch_u32;
+  uint32_t* status = doff + (int64_t)np * RS_BINS;
+  int* tickets = (int*)(status + (int64_t)np * tiles * RS_BINS);
+  int* own_err = tickets + np;
+  if (!err) err = own_err;
+  GH_CUDA_TRY(cudaMemsetAsync(doff, 0, sizeof(uint32_t) * ((int64_t)np * RS_BINS * (1 + tiles) + np + 1), st));
+  // pass q sorts word w = words-1-q/passes on digit q%passes
+  const unsigned hb = (unsigned)(tiles < 2 * 152 ? tiles : 2 * 152);
+  for (int w = words - 1; w >= 0; w--) {
+    os_hist_kernel<<<hb, RS_THREADS, 0, st>>>(keys + (int64_t)w * n, n, passes,
+                                              doff + (int64_t)(words - 1 - w) * passes * RS_BINS);
+    GH_LAUNCH_CHECK();
+  }
+  os_offsets_kernel<<<1, RS_BINS, 0, st>>>(doff, np);
+  GH_LAUNCH_CHECK();
   uint64_t *ks = keys, *kd = keys_tmp;
   uint32_t *is = idx, *id = idx_tmp;
-  for (int w = words - 1; w >= 0; w--) {
-    for (int p = 0; p < passes; p++) {
-      const int shift = 8 * p;
-      rs_hist_kernel<<<nb, RS_THREADS, 0, st>>>(ks + (int64_t)w * n, n, shift, scratch_u32, nb);
-      GH_LAUNCH_CHECK();
-      {
-        const int64_t m = (int64_t)RS_BINS * nb;
-        int* table = (int*)scratch_u32;
-        GH_TRY(exclusive_scan_i32(table, table, m, table + m + 1, st));
-      }
-      rs_scatter_kernel<<<nb, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, scratch_u32, nb);
-      GH_LAUNCH_CHECK();
-      uint64_t* tk = ks;
-      ks = kd;
-      kd = tk;
-      uint32_t* ti = is;
-      is = id;
-      id = ti;
-    }
+  for (int q = 0; q < np; q++) {
+    const int w = words - 1 - q / passes, shift = 8 * (q % passes);
+    os_pass_kernel<<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift,
+                                                           doff + (int64_t)q * RS_BINS,
+                                                           status + (int64_t)q * tiles * RS_BINS, tickets + q, err);
+    GH_LAUNCH_CHECK();
+    uint64_t* tk = ks;
+    ks = kd;
+    kd = tk;
+    uint32_t* ti = is;
+    is = id;
+    id = ti;
   }
   if (ks != keys) {
     GH_CUDA_TRY(cudaMemcpyAsync(keys, ks, sizeof(uint64_t) * words * n, cudaMemcpyDeviceToDevice, st));

@@ -15,10 +15,12 @@ constexpr int RS_BINS = 256;                       // 8-bit digits
 // word-major: key word w of item i at keys[w*n + i]) together with `idx`, stably.
 // Only the low `bits_per_word` bits of each word are examined.  `keys_tmp`/`idx_tmp`
 // are scratch of the same sizes.  On return the sorted data is in keys/idx.
-// `scratch_u32` must hold radix_scratch_words(n) entries.
+// `scratch_u32` must hold radix_scratch_words(n) entries.  At most 6 words.  A
+// bounded wait that gave up sets *err (device int; NULL: a flag in the scratch) and
+// leaves the result undefined.
 int64_t radix_scratch_words(int64_t n);
 int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t* idx_tmp, int words,
-                    int bits_per_word, int64_t n, uint32_t* scratch_u32, cudaStream_t st);
+                    int bits_per_word, int64_t n, uint32_t* scratch_u32, cudaStream_t st, int* err = nullptr);
 
 // Exclusive scan of in[0..n) into out[0..n] (out[n] = total).  `scratch` must hold
 // scan_scratch_ints(n) entries.  out may alias in.

@@ -738,7 +738,7 @@ struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
   Buffer nA, nC, nM, nF, parent, nchild, arrive, xh[2];
   Buffer list;                // particle lists: key fallbacks, then cell openers
-  int* host_flags = nullptr;  // pinned: tie, maxdepth, long run, nnodes
+  int* host_flags = nullptr;  // pinned: the 8 device flags, then nnodes
   int words = TREE_MIN_WORDS;
   int64_t full_sort_n = -1;  // particle count whose last build needed the full multi-word sort
 };
@@ -766,7 +766,7 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
                       cudaStream_t st, BuiltTree* out) {
   // int32 node indices: at most 127 cells per particle
   if (n > (1LL << 24)) return set_error(GH_ERR_ARG, "tree: at most 16777216 particles (got %lld)", (long long)n);
-  if (!ws.host_flags) GH_CUDA_TRY(cudaMallocHost((void**)&ws.host_flags, 4 * sizeof(int)));
+  if (!ws.host_flags) GH_CUDA_TRY(cudaMallocHost((void**)&ws.host_flags, 16 * sizeof(int)));
   const int T = 256;
   // 1. root cell
   GH_TRY(ensure(ws.part, BB_BLOCKS * 6 * sizeof(double)));
@@ -784,7 +784,8 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.depth, n * sizeof(int)));
   GH_TRY(ensure(ws.base, (n + 1) * sizeof(int)));
   GH_TRY(ensure(ws.scan, scan_scratch_ints(n) * sizeof(int)));
-  // flags: [0] full-key tie, [1] deepest level, [2] long run, [3] key fallbacks, [4] cell openers
+  // flags: [0] full-key tie, [1] deepest level, [2] long run, [3] key fallbacks, [4] cell openers,
+  // [5] a bounded wait in the sort gave up
   GH_TRY(ensure(ws.flags, 8 * sizeof(int)));
   GH_TRY(ensure(ws.list, n * sizeof(int)));
   GH_TRY(ensure(ws.idx, n * sizeof(uint32_t)));
@@ -810,9 +811,9 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
                                                                 flags + 3);
     GH_LAUNCH_CHECK();
     if (full_sort) {
-      GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, words, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
+      GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, words, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st, flags + 5));
     } else {
-      GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, 1, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st));
+      GH_TRY(radix_sort_keys(keys, idx, ktmp, itmp, 1, KEY_BITS, n, (uint32_t*)ws.rs.ptr, st, flags + 5));
       gather_words_kernel<<<gn, T, 0, st>>>(keys, ktmp, words, n, idx);
       GH_LAUNCH_CHECK();
       GH_CUDA_TRY(cudaMemcpyAsync(keys + n, ktmp + n, (size_t)(words - 1) * n * sizeof(uint64_t),
@@ -828,10 +829,11 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
                                    (int*)ws.flags.ptr);
     GH_LAUNCH_CHECK();
     GH_TRY(exclusive_scan_i32((const int*)ws.cnt.ptr, (int*)ws.base.ptr, n, (int*)ws.scan.ptr, st));
-    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 3 * sizeof(int), cudaMemcpyDeviceToHost, st));
-    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 3, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 8, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
                                 st));
     GH_CUDA_TRY(cudaStreamSynchronize(st));
+    if (ws.host_flags[5]) return set_error(GH_ERR_TIMEOUT, "tree: radix sort look-back gave up");
     if (ws.host_flags[2] && !full_sort) {  // a long run of equal first words
       full_sort = true;
       ws.full_sort_n = n;
@@ -846,7 +848,7 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   }
   const int words = ws.words;
   const int maxdepth = ws.host_flags[1];
-  const int nnodes = ws.host_flags[3];
+  const int nnodes = ws.host_flags[8];
   // 4. nodes
   GH_TRY(ensure(ws.nA, (size_t)nnodes * sizeof(WalkRec)));
   GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));
