@@ -58,6 +58,7 @@ constexpr uint32_t OS_INC = 2u << 30;    // status word: inclusive prefix publis
 constexpr uint32_t OS_VAL = (1u << 30) - 1;
 constexpr int OS_MAX_SPINS = 1 << 24;
 constexpr int OS_MAX_PASSES = 8;        // 8-bit digits of one 64-bit word
+constexpr int OS_WIN = 8;               // predecessor tiles read per look-back step
 
 __device__ __forceinline__ uint32_t ld_status(const uint32_t* p) { return *(const volatile uint32_t*)p; }
 __device__ __forceinline__ void st_status(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
@@ -137,19 +138,27 @@ __global__ void __launch_bounds__(RS_THREADS)
     st_status(my, OS_INC | cnt);
   } else {
     st_status(my, OS_AGG | cnt);
-    for (int t = tile - 1; t >= 0; t--) {
-      const uint32_t* ps = status + (int64_t)t * RS_BINS + tid;
-      uint32_t v = ld_status(ps);
-      for (int spin = 0; (v >> 30) == 0; spin++) {
-        if (spin >= OS_MAX_SPINS) {
-          atomicOr(err, 1);
-          v = OS_INC;
-          break;
+    // look back OS_WIN tiles at a time (independent loads), nearest first
+    bool done = false;
+    for (int t0 = tile - 1; t0 >= 0 && !done; t0 -= OS_WIN) {
+      uint32_t v[OS_WIN];
+#pragma unroll
+      for (int j = 0; j < OS_WIN; j++) v[j] = t0 - j >= 0 ? ld_status(status + (int64_t)(t0 - j) * RS_BINS + tid) : OS_INC;
+#pragma unroll
+      for (int j = 0; j < OS_WIN; j++) {
+        if (done) break;
+        const uint32_t* ps = status + (int64_t)(t0 - j) * RS_BINS + tid;
+        for (int spin = 0; (v[j] >> 30) == 0; spin++) {
+          if (spin >= OS_MAX_SPINS) {
+            atomicOr(err, 1);
+            v[j] = OS_INC;
+            break;
+          }
+          v[j] = ld_status(ps);
         }
-        v = ld_status(ps);
+        excl += v[j] & OS_VAL;
+        done = (v[j] & ~OS_VAL) == OS_INC;
       }
-      excl += v & OS_VAL;
-      if ((v & ~OS_VAL) == OS_INC) break;
     }
     st_status(my, OS_INC | (excl + cnt));
   }
