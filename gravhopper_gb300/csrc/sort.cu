@@ -99,7 +99,11 @@ __global__ void __launch_bounds__(RS_BINS) os_offsets_kernel(uint32_t* __restric
   }
 }
 
-__global__ void __launch_bounds__(RS_THREADS)
+// WK = 1 or 2: the tile's key words and payloads are loaded into registers, all
+// loads issued together, before the digits are counted; WK = 0: any number of
+// words, the digit word loaded first and the rest reloaded per round.
+template <int WK>
+__global__ void __launch_bounds__(RS_THREADS, 2)
     os_pass_kernel(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ iin, uint64_t* __restrict__ kout,
                    uint32_t* __restrict__ iout, int words, int64_t n, int w, int shift,
                    const uint32_t* __restrict__ doff, uint32_t* __restrict__ status, int* __restrict__ ticket,
@@ -122,10 +126,24 @@ __global__ void __launch_bounds__(RS_THREADS)
   const int64_t base = (int64_t)tile * RS_TILE;
   const uint64_t* kw = kin + (int64_t)w * n;
   unsigned dig[RS_ROUNDS];
+  uint64_t kr[RS_ROUNDS][WK > 0 ? WK : 1];
+  uint32_t ir[RS_ROUNDS];
 #pragma unroll
   for (int r = 0; r < RS_ROUNDS; r++) {
     const int64_t i = base + r * RS_THREADS + tid;
-    dig[r] = i < n ? (unsigned)((kw[i] >> shift) & 255u) : 256u;
+    if (WK > 0) {
+#pragma unroll
+      for (int q = 0; q < (WK > 0 ? WK : 1); q++) kr[r][q] = i < n ? kin[(int64_t)q * n + i] : 0ull;
+      ir[r] = i < n ? iin[i] : 0u;
+    } else {
+      kr[r][0] = i < n ? kw[i] : 0ull;
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < RS_ROUNDS; r++) {
+    const int64_t i = base + r * RS_THREADS + tid;
+    const uint64_t kd = (WK == 2 && w == 1) ? kr[r][WK > 1 ? 1 : 0] : kr[r][0];  // no dynamic register index
+    dig[r] = i < n ? (unsigned)((kd >> shift) & 255u) : 256u;
     const unsigned peers = __match_any_sync(0xffffffffu, dig[r]);
     if (dig[r] < 256u && (peers & lanemask_lt()) == 0) atomicAdd(&tile_cnt[dig[r]], (uint32_t)__popc(peers));
   }
@@ -188,8 +206,14 @@ __global__ void __launch_bounds__(RS_THREADS)
     __syncthreads();
     if (valid) {
       const int64_t pos = (int64_t)cursor[d] + warp_off[warp][d] + rank;
-      for (int q = 0; q < words; q++) kout[(int64_t)q * n + pos] = kin[(int64_t)q * n + i];
-      iout[pos] = iin[i];
+      if (WK > 0) {
+#pragma unroll
+        for (int q = 0; q < (WK > 0 ? WK : 1); q++) kout[(int64_t)q * n + pos] = kr[r][q];
+        iout[pos] = ir[r];
+      } else {
+        for (int q = 0; q < words; q++) kout[(int64_t)q * n + pos] = kin[(int64_t)q * n + i];
+        iout[pos] = iin[i];
+      }
     }
     __syncthreads();
     cursor[tid] += round_tot[tid];
@@ -233,9 +257,17 @@ int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t*
   uint32_t *is = idx, *id = idx_tmp;
   for (int q = 0; q < np; q++) {
     const int w = words - 1 - q / passes, shift = 8 * (q % passes);
-    os_pass_kernel<<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift,
-                                                           doff + (int64_t)q * RS_BINS,
-                                                           status + (int64_t)q * tiles * RS_BINS, tickets + q, err);
+    const uint32_t* dq = doff + (int64_t)q * RS_BINS;
+    uint32_t* sq = status + (int64_t)q * tiles * RS_BINS;
+    if (words == 1)
+      os_pass_kernel<1><<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, dq, sq, tickets + q,
+                                                                err);
+    else if (words == 2)
+      os_pass_kernel<2><<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, dq, sq, tickets + q,
+                                                                err);
+    else
+      os_pass_kernel<0><<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, dq, sq, tickets + q,
+                                                                err);
     GH_LAUNCH_CHECK();
     uint64_t* tk = ks;
     ks = kd;
