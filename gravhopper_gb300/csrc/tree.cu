@@ -386,6 +386,7 @@ struct NodeArrays {
   dvec4* F;      // (first moment x, y, z, mass)          build only
   int* parent;   // enclosing cell, -1 for the root        build only
   int* nchild;   // number of child cells                  build only
+  int* kids;     // child cell per octant (8 per cell, -1 none)  build only
   int* arrive;   // children whose monopole is done        build only
 };
 
@@ -400,6 +401,14 @@ __device__ __forceinline__ int64_t cell_end(const uint64_t* __restrict__ keys, i
   for (int s = 0; s < 16; s++, j++)
     if (lp[j] < L) return j;  // lp[n] = -1 ends the scan
   int64_t a = j - 1, b = n - 1;  // a shares >= L digits with i
+  // gallop: most cells are small, so bracket the end before bisecting
+  for (int64_t step = 32; a + step < b; step *= 2) {
+    if (key_lcp(keys, words, n, i, a + step) < L) {
+      b = a + step - 1;
+      break;
+    }
+    a += step;
+  }
   while (a < b) {
     const int64_t mid = (a + b + 1) >> 1;
     if (key_lcp(keys, words, n, i, mid) >= L)
@@ -417,6 +426,13 @@ __device__ __forceinline__ int64_t cell_begin(const uint64_t* __restrict__ keys,
   for (int s = 0; s < 16; s++, j--)
     if (lp[j] < L) return j;  // lp[0] = -1 ends the scan
   int64_t a = 0, b = j;  // b shares >= L digits with i
+  for (int64_t step = 32; b - step > a; step *= 2) {
+    if (key_lcp(keys, words, n, b - step, i) < L) {
+      a = b - step + 1;
+      break;
+    }
+    b -= step;
+  }
   while (a < b) {
     const int64_t mid = (a + b) >> 1;
     if (key_lcp(keys, words, n, mid, i) >= L)
@@ -452,7 +468,10 @@ __global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64
       const int k = k0 + (L - lo);
       const int pk = L == lo ? par : k - 1;
       na.parent[k] = pk;
-      if (pk >= 0) atomicAdd(&na.nchild[pk], 1);
+      if (pk >= 0) {
+        atomicAdd(&na.nchild[pk], 1);
+        na.kids[8 * pk + key_digit(keys, n, i, L - 1)] = k;
+      }
     }
     const int k = k0 + (d - lo);
     const int next = i + 1 < n ? base[i + 1] : nnodes;
@@ -478,6 +497,7 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
     const int64_t i = list[q];
     const int lo = lp[i] + 1, d = depth[i];
     const int k0 = base[i];
+    const uint64_t kw0 = keys[i], kw1 = words > 1 ? keys[n + i] : 0ull;  // digits of the first 42 levels
     double c[3] = {root->c[0], root->c[1], root->c[2]};
     for (int L = 0; L < d; L++) {
       if (L >= lo) {
@@ -499,7 +519,9 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
         na.C[k] = make_dvec4(c[0], c[1], c[2], size);
       }
       if (L + 1 < d) {
-        const unsigned g = key_digit(keys, n, i, L);
+        const unsigned g = L < KEY_LEVELS       ? (unsigned)(kw0 >> (3 * (KEY_LEVELS - 1 - L))) & 7u
+                           : L < 2 * KEY_LEVELS ? (unsigned)(kw1 >> (3 * (2 * KEY_LEVELS - 1 - L))) & 7u
+                                                : key_digit(keys, n, i, L);
         const double off = offs[L];
 #pragma unroll
         for (int r = 0; r < 3; r++) c[r] = ((g >> r) & 1u) ? dadd(c[r], off) : dsub(c[r], off);
@@ -517,6 +539,12 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
 // depend on which child arrives last, so the result is deterministic.
 __device__ __forceinline__ int node_next(const WalkRec* __restrict__ R, int k) { return __float_as_int(R[k].L.w); }
 
+
+__device__ __forceinline__ int atomic_add_acq_rel(int* p, int v) {
+  int old;
+  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
+  return old;
+}
 
 // 1/m from the hardware approximation and two Newton steps y <- y + y (1 - m y).
 __device__ __forceinline__ double rcp_f64(double m) {
@@ -548,13 +576,18 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
   for (;;) {
     const int par = na.parent[cur];
     if (par < 0) break;
-    __threadfence();  // this child's moments before its arrival
-    if (atomicAdd(&na.arrive[par], 1) != na.nchild[par] - 1) break;
-    __threadfence();  // every sibling's moments after the last arrival
-    const int nx = node_next(na.R, par);
+    // release this child's moments, acquire the siblings' (one acq_rel RMW on the counter)
+    if (atomic_add_acq_rel(&na.arrive[par], 1) != na.nchild[par] - 1) break;
+    // children in preorder = in octant order; their slots are known, so the loads of
+    // their moments are independent
+    const int4 ka = reinterpret_cast<const int4*>(na.kids)[2 * par];
+    const int4 kb = reinterpret_cast<const int4*>(na.kids)[2 * par + 1];
+    const int kid[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
     double fx = 0.0, fy = 0.0, fz = 0.0, m = 0.0;
-    for (int c = par + 1; c < nx; c = node_next(na.R, c)) {
-      const double2* f = reinterpret_cast<const double2*>(na.F + c);
+#pragma unroll
+    for (int o = 0; o < 8; o++) {
+      if (kid[o] < 0) continue;
+      const double2* f = reinterpret_cast<const double2*>(na.F + kid[o]);
       const double2 fa = __ldcg(f), fb = __ldcg(f + 1);  // siblings were written by other threads
       fx = dadd(fx, fa.x);
       fy = dadd(fy, fa.y);
@@ -736,7 +769,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
 // ---------------------------------------------------------------------------
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
-  Buffer nA, nC, nM, nF, parent, nchild, arrive, xh[2];
+  Buffer nA, nC, nM, nF, parent, nchild, arrive, kids, xh[2];
   Buffer list;                // particle lists: key fallbacks, then cell openers
   int* host_flags = nullptr;  // pinned: the 8 device flags, then nnodes
   int words = TREE_MIN_WORDS;
@@ -753,6 +786,7 @@ static NodeArrays node_arrays(TreeWS& ws) {
   na.F = (dvec4*)ws.nF.ptr;
   na.parent = (int*)ws.parent.ptr;
   na.nchild = (int*)ws.nchild.ptr;
+  na.kids = (int*)ws.kids.ptr;
   na.arrive = (int*)ws.arrive.ptr;
   return na;
 }
@@ -857,9 +891,11 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.parent, (size_t)nnodes * sizeof(int)));
   GH_TRY(ensure(ws.nchild, (size_t)nnodes * sizeof(int)));
   GH_TRY(ensure(ws.arrive, (size_t)nnodes * sizeof(int)));
+  GH_TRY(ensure(ws.kids, (size_t)nnodes * 8 * sizeof(int)));
   NodeArrays na = node_arrays(ws);
   GH_CUDA_TRY(cudaMemsetAsync(ws.nchild.ptr, 0, (size_t)nnodes * sizeof(int), st));
   GH_CUDA_TRY(cudaMemsetAsync(ws.arrive.ptr, 0, (size_t)nnodes * sizeof(int), st));
+  GH_CUDA_TRY(cudaMemsetAsync(ws.kids.ptr, 0xff, (size_t)nnodes * 8 * sizeof(int), st));
   {
     const uint64_t* keys = (const uint64_t*)ws.keys.ptr;
     const int* lp = (const int*)ws.lp.ptr;
