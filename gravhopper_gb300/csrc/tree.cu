@@ -649,6 +649,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
   }
   const float h0 = (float)p0, h1 = (float)p1, h2 = (float)p2;
   const float l0 = f32_lo(p0, h0), l1 = f32_lo(p1, h1), l2 = f32_lo(p2, h2);
+  const f2 h01 = f2make(h0, h1), l01 = f2make(l0, l1);
   // d^2 below this needs the exact test: FP32 differences lose too much relative to
   // |x|, and FP32 stays in its normal range (with theta >= 1e-3 a cell whose size^2
   // is below that range is then accepted, as the exact test would)
@@ -672,9 +673,11 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       if (MIXED) O = nR[node].O;
       const int nx = __float_as_int(Lo.w);
       bool accept = (nx == node + 1);  // leaf
-      const float dx = (A.x - h0) + (Lo.x - l0);
-      const float dy = (A.y - h1) + (Lo.y - l1);
+      // (x, y) offsets as one f32x2 pair, z alone
+      const f2 dxy = f2add(f2sub(f2make(A.x, A.y), h01), f2sub(f2make(Lo.x, Lo.y), l01));
       const float dz = (A.z - h2) + (Lo.z - l2);
+      float dx, dy;
+      f2split(dxy, dx, dy);
       if (!accept) {
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float s2 = A.w;
@@ -700,7 +703,9 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
           if (nx == node + 1) n_leaf++;
         }
         if (MIXED) {
-          const float ex = dx + O.x, ey = dy + O.y, ez = dz + O.z;
+          float ex, ey;
+          f2split(f2add(dxy, f2make(O.x, O.y)), ex, ey);
+          const float ez = dz + O.z;
           const float s = fmaf(ex, ex, fmaf(ey, ey, fmaf(ez, ez, eps2f)));
           float r = rsqrt_approx(s);
           if (GUARD) r = s > 0.f ? r : 0.f;
