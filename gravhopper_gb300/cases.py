@@ -2,6 +2,7 @@
 
     python -m gravhopper_gb300.cases direct   --n 131072 --reps 2   # mixed direct force
     python -m gravhopper_gb300.cases direct64 --n 65536  --reps 1   # FP64 direct force
+    python -m gravhopper_gb300.cases dkd      --n 1048576 --reps 1  # mixed DKD step
     python -m gravhopper_gb300.cases tree     --n 65536  --theta 0.7 --precision fp64
     python -m gravhopper_gb300.cases ensemble --systems 64
     python -m gravhopper_gb300.cases vjp      --n 16384
@@ -18,7 +19,7 @@ import time
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("case", choices=["direct", "direct64", "tree", "ensemble", "vjp"])
+    ap.add_argument("case", choices=["direct", "direct64", "dkd", "tree", "ensemble", "vjp"])
     ap.add_argument("--n", type=int, default=131072)
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--theta", type=float, default=0.7)
@@ -36,7 +37,7 @@ def main(argv=None):
     _capi.load()
     _capi.call("gh_direct_set_fp64_form", a.fp64_form)
     _capi.call("gh_direct_set_shape", a.shape)
-    if a.case in ("direct", "direct64", "vjp"):
+    if a.case in ("direct", "direct64", "dkd", "vjp"):
         ic = ics.plummer(a.n, seed=0)
     elif a.case == "tree":
         ic = ics.hernquist_disk(a.n, seed=1)
@@ -49,6 +50,9 @@ def main(argv=None):
         m = torch.from_numpy(ic["mass"]).to(dev)
         if a.case == "direct":
             call = lambda: engine.direct_force(x, m, 5e-5, precision="mixed")  # noqa: E731
+        elif a.case == "dkd":  # one leapfrog step with the mixed direct sum (the bench's step)
+            v = torch.from_numpy(ic["vel"]).to(dev)
+            call = lambda: engine.run_dkd(x, v, m, 1, 0.005, 5e-5, precision="mixed")  # noqa: E731
         elif a.case == "direct64":
             call = lambda: engine.direct_force(x, m, 5e-5, precision="fp64")  # noqa: E731
         elif a.case == "tree":
