@@ -250,9 +250,13 @@ def main():
     kern_avg_s = kern_ms / max(kern_n, 1) * 1e-3
     achieved = pairs / kern_avg_s / 1e9
     peak = fp32_peak / PAIR_OPS / 1e9
+    # DRAM bytes (read + write) of one launch of the fused DKD kernel at N = 1,048,576,
+    # from one single-pass ncu capture (dram__bytes_read.sum 78.47 MB + write 29.32 MB;
+    # profiles/direct_mixed_bench_n1048576_launches.md); other sizes: not captured
+    traffic = 107.79e6 if (args.precision == "mixed" and n == 1 << 20) else None
     roofline = {"bound": "fp32", "kernel": "direct_mixed_kernel" if args.precision == "mixed" else
                 "direct_f64_kernel", "achieved": achieved, "peak": peak, "unit": UNIT,
-                "frac": achieved / peak, "traffic": None,
+                "frac": achieved / peak, "traffic": traffic,
                 "peak_source": f"measured live: f32x2 FMA chains, {fp32_peak / 1e12:.1f} T lane-op/s "
                                f"/ {PAIR_OPS} lane-ops per pair",
                 "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
