@@ -595,15 +595,29 @@ __global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ 
       m = dadd(m, fb.y);
     }
     na.F[par] = make_dvec4(fx, fy, fz, m);
-    // firstmoment / mass (_jbgrav.c:478) as a product with a Newton-refined reciprocal:
-    // within an ulp or two of the quotient, at a third of the FP64 work of three
-    // divisions (this loop runs on few lanes of a warp)
-    const double r = rcp_f64(m);
-    const double cx = dmul(fx, r), cy = dmul(fy, r), cz = dmul(fz, r);
-    na.M[par] = make_dvec4(cx, cy, cz, m);
-    const dvec4 C = na.C[par];
-    na.R[par].O = make_float4((float)dsub(cx, C.x), (float)dsub(cy, C.y), (float)dsub(cz, C.z), (float)m);
     cur = par;
+  }
+}
+
+// Centres of mass of the internal cells, on full warps (the climb above runs on few
+// lanes per warp, and GB300 issues FP64 at 1/74 of the FP32 rate): firstmoment / mass
+// (_jbgrav.c:478) as a product with a Newton-refined reciprocal, within an ulp or two of
+// the quotient.  The listed particles are the ones that opened internal cells.
+__global__ void com_final_kernel(NodeArrays na, const int* __restrict__ lp, const int* __restrict__ depth,
+                                 const int* __restrict__ base, const int* __restrict__ list,
+                                 const int* __restrict__ count) {
+  const int cnt = *count;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
+    const int64_t i = list[q];
+    const int k0 = base[i], internal = depth[i] - (lp[i] + 1);  // cells k0 .. k0+internal-1
+    for (int k = k0; k < k0 + internal; k++) {
+      const dvec4 F = na.F[k];
+      const double r = rcp_f64(F.w);
+      const double cx = dmul(F.x, r), cy = dmul(F.y, r), cz = dmul(F.z, r);
+      na.M[k] = make_dvec4(cx, cy, cz, F.w);
+      const dvec4 C = na.C[k];
+      na.R[k].O = make_float4((float)dsub(cx, C.x), (float)dsub(cy, C.y), (float)dsub(cz, C.z), (float)F.w);
+    }
   }
 }
 
@@ -916,6 +930,10 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   // 5. monopoles
   com_up_kernel<<<gn, T, 0, st>>>(na, n, (const int*)ws.lp.ptr, (const int*)ws.depth.ptr, (const int*)ws.base.ptr,
                                   (const uint32_t*)ws.idx.ptr, pos, mass);
+  GH_LAUNCH_CHECK();
+  com_final_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(na, (const int*)ws.lp.ptr, (const int*)ws.depth.ptr,
+                                                              (const int*)ws.base.ptr, (const int*)ws.list.ptr,
+                                                              (const int*)ws.flags.ptr + 4);
   GH_LAUNCH_CHECK();
   out->nnodes = nnodes;
   out->maxdepth = maxdepth;
