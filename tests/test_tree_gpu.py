@@ -168,6 +168,22 @@ def test_mixed_tree_against_reference_golden(golden, lib, cuda, theta):
         check(got, ref, MIXED_TREE_RMS_TOL, MIXED_TREE_MAX_TOL)
 
 
+@pytest.mark.parametrize("theta", [0.5, 0.7])
+def test_mixed_tree_zero_softening_and_targets(golden, lib, cuda, theta):
+    """Mixed walk with eps = 0 (a target on a particle gets no term from it, as the
+    reference's r^2 + eps^2 == 0 rule) at target points."""
+    import torch
+
+    from gravhopper_gb300 import engine
+    key = str(theta).replace(".", "p")
+    x = torch.from_numpy(golden["tree_pos"]).to(cuda)
+    m = torch.from_numpy(golden["tree_mass"]).to(cuda)
+    fp = torch.from_numpy(golden["tree_fpos"]).to(cuda)
+    got = engine.tree_force(x, m, 0.0, theta, force_pos=fp, precision="mixed").cpu().numpy()
+    assert np.isfinite(got).all()
+    check(got, golden[f"treepos_{key}_out"], MIXED_TREE_RMS_TOL, MIXED_TREE_MAX_TOL)
+
+
 def test_mixed_tree_large_against_oracle(lib, cuda):
     import torch
 
