@@ -104,9 +104,12 @@ static int g_f64_form = -1;  // -1 by target count, 0 thread per target, 1 order
 
 // Measured on GB300 (pairs/s per shape at N = 2000, 16384, 1048576): small systems
 // want small tiles (more CTAs share the sources), large ones the widest CTAs.
-static int auto_shape(int64_t np, int64_t nt) {
+// Large N, scalar FP32 loop: the fused leapfrog step (heavier epilogue) runs fastest
+// with 384 threads x 6 targets (435 ms per step at N = 1M against 443 ms), a plain
+// force with 512 threads x 4 targets (443 ms against 454 ms).
+static int auto_shape(int64_t np, int64_t nt, bool dkd) {
   const int64_t n = np > nt ? np : nt;
-  if (n >= (1 << 19)) return 10;  // 512 threads, 4 targets per thread, scalar FP32 loop
+  if (n >= (1 << 19)) return dkd ? 12 : 10;
   if (n >= 8192) return 3;       // 128 threads, 2 packs, 4 CTAs/SM
   return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
 }
@@ -235,7 +238,7 @@ static int launch_mixed(DirectWS& ws, const float4* src, int64_t np, const float
   GH_TRY(device_info(&di));
   const float eps2 = (float)(eps * eps);
   const bool guard = !(eps2 > 0.f);
-  const int shape = g_mixed_shape >= 0 ? g_mixed_shape : auto_shape(np, nt);
+  const int shape = g_mixed_shape >= 0 ? g_mixed_shape : auto_shape(np, nt, Epi::kFusedStep);
   const MixedShape ms = kMixedShapes[shape];
   StreamK sk = mixed_plan(np, nt, mixed_grid_cap(di.num_sms, shape, guard), ms.threads * 2 * ms.packs,
                           ms.threads);

@@ -67,6 +67,7 @@ __device__ __forceinline__ double kick(double v, double a_code, double dt) {
 
 // Store the acceleration (code units) into acc[(N,3)].
 struct EpiStore {
+  static constexpr bool kFusedStep = false;
   double* acc;
   __device__ __forceinline__ void operator()(int64_t i, double ax, double ay, double az) const {
     acc[3 * i + 0] = ax;
@@ -81,6 +82,7 @@ struct EpiStore {
 //              mixed form, or FP64 (N,3) in `xh_next` for the FP64 form
 //   hist_x/v : optional snapshot slots (N,3) written with the new state
 struct EpiDKD {
+  static constexpr bool kFusedStep = true;
   double* x;
   double* v;
   const double* mass;
