@@ -116,3 +116,14 @@ def energy(pos, vel, mass, eps):
     ke = 0.5 * float(torch.sum(mass * torch.sum(vel * vel, dim=1)))
     pe = 0.5 * G_KPC_KMS2_MSUN * float(torch.sum(mass * potential(pos, mass, eps)))
     return ke, pe, ke + pe
+
+
+def momentum(pos, vel, mass):
+    """Total linear momentum (3,) in Msun km/s and angular momentum about the origin
+    (3,) in Msun kpc km/s, FP64 sums on the device."""
+    _check(pos, "pos", 3)
+    _check(vel, "vel", 3)
+    _check(mass, "mass")
+    p = torch.sum(mass[:, None] * vel, dim=0)
+    lm = torch.sum(mass[:, None] * torch.linalg.cross(pos, vel, dim=1), dim=0)
+    return p, lm

@@ -110,3 +110,26 @@ def test_simulation_with_external_force_matches_restatement(golden, lib, cuda):
         x = xh + ((0.5 * v) * 0.005) * oracle.KMS_MYR_TO_KPC
     np.testing.assert_array_equal(sim.positions[6], x)
     np.testing.assert_array_equal(sim.velocities[6], v)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_momentum_diagnostics_conserved(lib, cuda, precision):
+    """Pairwise central forces conserve linear and angular momentum; the leapfrog keeps
+    both to rounding.  engine.momentum matches a host sum."""
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    ic = ics.plummer(4096, seed=21)
+    x = torch.from_numpy(ic["pos"]).to(cuda)
+    v = torch.from_numpy(ic["vel"]).to(cuda)
+    m = torch.from_numpy(ic["mass"]).to(cuda)
+    p0, l0 = engine.momentum(x, v, m)
+    np.testing.assert_allclose(p0.cpu().numpy(), np.sum(ic["mass"][:, None] * ic["vel"], axis=0), rtol=0,
+                               atol=1e-9 * float(np.sum(ic["mass"] * np.linalg.norm(ic["vel"], axis=1))))
+    scale_p = float(torch.sum(m * torch.linalg.norm(v, dim=1)))
+    scale_l = float(torch.sum(m * torch.linalg.norm(x, dim=1) * torch.linalg.norm(v, dim=1)))
+    engine.run_dkd(x, v, m, 50, 0.005, 5e-5, precision=precision)
+    p1, l1 = engine.momentum(x, v, m)
+    tol = 1e-12 if precision == "fp64" else 1e-6
+    assert float(torch.linalg.norm(p1 - p0)) <= tol * scale_p
+    assert float(torch.linalg.norm(l1 - l0)) <= tol * scale_l
