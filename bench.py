@@ -49,7 +49,7 @@ def parse():
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-secondary", action="store_true")
-    ap.add_argument("--cpu-targets", type=int, default=4096,
+    ap.add_argument("--cpu-targets", type=int, default=49152,
                     help="targets in the CPU-baseline sample (each against all N sources)")
     ap.add_argument("--report", choices=["config0", "config1", "config4"],
                     help="print one JSON line of the full measurements for that workload instead")
@@ -139,7 +139,7 @@ def run_reference(args):
         return
     res = []
     for k in range(args.warmup + args.steps):
-        r = cpu_baseline(args.n, max(64, args.cpu_targets // 2), seed=k)
+        r = cpu_baseline(args.n, max(64, min(args.cpu_targets, 8192) // 2), seed=k)  # ~0.4 s per step
         if k >= args.warmup:
             res.append(r)
     val = statistics.median(r["value"] for r in res)
