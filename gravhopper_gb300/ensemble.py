@@ -70,7 +70,8 @@ def autotune(ens: Ensemble, steps=4, use_cache=True):
     Returns (best_config, {config: ms_per_step}).  Results are cached per device
     name and ensemble signature.
     """
-    key = f"{torch.cuda.get_device_name(ens.device)}|ensemble|{ens.signature()}"
+    nconf = int(_capi.load().gh_ensemble_num_configs())
+    key = f"{torch.cuda.get_device_name(ens.device)}|ensemble|{nconf} configs|{ens.signature()}"
     path = _cache_path()
     cache = {}
     if use_cache and os.path.exists(path):
@@ -84,7 +85,7 @@ def autotune(ens: Ensemble, steps=4, use_cache=True):
             return ens.config, {int(k): v for k, v in cache[key]["ms"].items()}
     saved = (ens.pos.clone(), ens.vel.clone())
     times = {}
-    for cfg in range(int(_capi.load().gh_ensemble_num_configs())):
+    for cfg in range(nconf):
         ens.pos.copy_(saved[0])
         ens.vel.copy_(saved[1])
         ens.run(1, config=cfg, use_graph=False)  # warm-up
