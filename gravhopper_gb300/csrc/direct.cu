@@ -102,16 +102,18 @@ static std::recursive_mutex g_mu;
 static int g_mixed_shape = -1;
 static int g_f64_form = -1;  // -1 by target count, 0 thread per target, 1 ordered CTA-wide terms
 
-// Measured on GB300 (pairs/s per shape at N = 2000, 16384, 1048576): small systems
-// want small tiles (more CTAs share the sources), large ones the widest CTAs.
-// Large N, scalar FP32 loop: the fused leapfrog step (heavier epilogue) runs fastest
-// with 384 threads x 6 targets (435 ms per step at N = 1M against 443 ms), a plain
-// force with 512 threads x 4 targets (443 ms against 454 ms).
+// Chosen from a sweep of the shapes on GB300 (force and fused leapfrog step, N = 2048
+// to 1M): small systems want small tiles (more CTAs share the sources); from N ~ 24k
+// the scalar FP32 loop with wide CTAs wins, 512 threads x 4 targets for a force at
+// every size (e.g. 1.78 ms against 1.93 ms for the packed 128 x 4 at N = 65,536) and
+// for the leapfrog step up to ~128k, 384 threads x 6 targets for larger steps, whose
+// heavier epilogue favours it (435 ms per step at N = 1M against 443 ms).
 static int auto_shape(int64_t np, int64_t nt, bool dkd) {
   const int64_t n = np > nt ? np : nt;
-  if (n >= (1 << 19)) return dkd ? 12 : 10;
-  if (n >= 8192) return 3;       // 128 threads, 2 packs, 4 CTAs/SM
-  return 7;                      // 256 threads, 1 pack, 4 CTAs/SM
+  if (n < 12288) return 7;                   // packed, 256 threads, 1 pack, 4 CTAs/SM
+  if (n < 24576) return 3;                   // packed, 128 threads, 2 packs, 4 CTAs/SM
+  if (dkd && n >= (1 << 17)) return 12;      // scalar, 384 threads x 6 targets
+  return 10;                                 // scalar, 512 threads x 4 targets
 }
 
 template <bool G, int T, int P, int B, class Epi, bool PK = true>
