@@ -695,7 +695,8 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       if (!accept) {
         const float d2 = fmaf(dz, dz, fmaf(dy, dy, dx * dx));
         const float s2 = A.w;
-        const bool usable = d2 > near2 && d2 < 1e30f;
+        // d2 = inf (overflow) accepts, as the exact test does for so distant a cell
+        const bool usable = d2 > near2;
         if (usable && s2 < th2_lo * d2) {
           accept = true;
         } else if (usable && s2 > th2_hi * d2) {
@@ -727,20 +728,6 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
           px = fmaf(f, ex, px);
           py = fmaf(f, ey, py);
           pz = fmaf(f, ez, pz);
-          if (++pending == TW_FOLD) {
-            float sx, ex;
-            two_sum(hx, px, sx, ex);
-            hx = sx;
-            qx += ex;
-            two_sum(hy, py, sx, ex);
-            hy = sx;
-            qy += ex;
-            two_sum(hz, pz, sx, ex);
-            hz = sx;
-            qz += ex;
-            px = py = pz = 0.f;
-            pending = 0;
-          }
         } else {
           const dvec4 M = nM[node];
           const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
@@ -758,6 +745,22 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       } else {
         lane_next = node + 1;
       }
+    }
+    // fold the FP32 partials every TW_FOLD warp steps (at most one interaction per
+    // target per step): a warp-uniform branch
+    if (MIXED && ++pending == TW_FOLD) {
+      float sx, ex;
+      two_sum(hx, px, sx, ex);
+      hx = sx;
+      qx += ex;
+      two_sum(hy, py, sx, ex);
+      hy = sx;
+      qy += ex;
+      two_sum(hz, pz, sx, ex);
+      hz = sx;
+      qz += ex;
+      px = py = pz = 0.f;
+      pending = 0;
     }
     node = __reduce_min_sync(0xffffffffu, lane_next);
   }
