@@ -79,6 +79,7 @@ SIGNATURES = {
     "gh_direct_vjp_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _int, _vp, _vp, _vp]),
     "gh_potential_dev": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_dkd_backward_dev": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _vp, _vp, _vp, _vp]),
+    "gh_dkd_backward_chain_dev": (_int, [_vp, _vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _int, _vp, _vp, _vp, _vp]),
     "gh_direct_num_shapes": (_int, []),
     "gh_direct_set_fp64_form": (_int, [_int]),
     "gh_kernel_timing": (_int, [_int]),

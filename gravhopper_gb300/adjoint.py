@@ -3,8 +3,9 @@
 ``rollout(x0, v0, m, nsteps, dt, eps)`` is a ``torch.autograd.Function``: the forward
 pass runs the drift-kick-drift leapfrog on the GPU (gravhopper/gravhopper.py:405-416
 arithmetic), keeping the state every ``checkpoint_every`` steps; the backward pass
-walks the segments in reverse and hands each to ``gh_dkd_backward_dev``, which
-recomputes the segment's states from its checkpoint and back-propagates step by step:
+hands all checkpoints to ``gh_dkd_backward_chain_dev``, which walks the segments in
+reverse, recomputing each segment's states from its checkpoint (on a second stream,
+while the following segment back-propagates) and back-propagating step by step:
 
     forward:  xh = x + c v,  a = A F(xh, m),  v' = v + dt a,  x' = xh + c v'
     backward: w = v'bar + c x'bar,  lam = A dt w,  (gx, gm) = VJP of F at xh with lam,
@@ -15,6 +16,8 @@ direct sum and its VJP the ``gh_direct_vjp_dev`` kernel (softened tidal tensor
 contracted with the cotangent, plus the mass gradient).
 """
 from __future__ import annotations
+
+import ctypes
 
 import torch
 
@@ -28,14 +31,14 @@ class _Rollout(torch.autograd.Function):
         v = v0.detach().clone().contiguous()
         md = m.detach().contiguous()
         k = max(1, int(checkpoint_every))
-        ckpts = []
-        done = 0
-        while done < nsteps:
-            seg = min(k, nsteps - done)
-            ckpts.append((x.clone(), v.clone(), seg))
+        segs = [min(k, nsteps - s0) for s0 in range(0, nsteps, k)]
+        cx = torch.empty((len(segs),) + tuple(x.shape), dtype=x.dtype, device=x.device)
+        cv = torch.empty_like(cx)
+        for q, seg in enumerate(segs):
+            cx[q].copy_(x)
+            cv[q].copy_(v)
             engine.run_dkd(x, v, md, seg, dt, eps, algorithm="direct", precision=precision)
-            done += seg
-        ctx.ckpts = ckpts
+        ctx.ckpts = (cx, cv, segs)
         ctx.params = (dt, eps, precision)
         ctx.save_for_backward(md)
         return x, v
@@ -48,10 +51,12 @@ class _Rollout(torch.autograd.Function):
         xb = gx.contiguous().clone() if gx is not None else torch.zeros((n, 3), dtype=torch.float64, device=m.device)
         vb = gv.contiguous().clone() if gv is not None else torch.zeros_like(xb)
         mb = torch.zeros_like(m)
-        for xs, vs, seg in reversed(ctx.ckpts):
-            _capi.call("gh_dkd_backward_dev", _capi.ptr(xs), _capi.ptr(vs), _capi.ptr(m), n, int(seg), float(dt),
-                       float(eps), _capi.PRECISIONS[precision], _capi.ptr(xb), _capi.ptr(vb), _capi.ptr(mb),
-                       _capi.stream_handle())
+        cx, cv, segs = ctx.ckpts
+        if segs:
+            seg_arr = (ctypes.c_int64 * len(segs))(*segs)
+            _capi.call("gh_dkd_backward_chain_dev", _capi.ptr(cx), _capi.ptr(cv), ctypes.addressof(seg_arr),
+                       len(segs), _capi.ptr(m), n, float(dt), float(eps), _capi.PRECISIONS[precision],
+                       _capi.ptr(xb), _capi.ptr(vb), _capi.ptr(mb), _capi.stream_handle())
         ctx.ckpts = None
         return xb, vb, mb, None, None, None, None, None
 

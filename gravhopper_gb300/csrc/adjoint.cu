@@ -457,9 +457,31 @@ __global__ void adj_post_kernel(int64_t n, double dt, const double* __restrict__
 
 struct BwdWS {
   Buffer states_x, states_v, work_x, work_v, xh, w, lam, gpos, gmass;
+  Buffer chain_x[2], chain_v[2];        // dkd_backward_chain: recomputed segments, two buffers
+  cudaStream_t rstream = nullptr;       // dkd_backward_chain: recomputation stream
+  cudaEvent_t ev[3] = {nullptr, nullptr, nullptr};
 };
 static BwdWS g_bwd[64];
 static std::mutex g_bwd_mu;
+
+// Back-propagates through `nsteps` recomputed states (sx, sv: state at the start of
+// each step) with the VJP kernel: (xbar, vbar) updated in place, mbar incremented.
+static int backward_steps(BwdWS& ws, const double* sx, const double* sv, const double* mass, int64_t n,
+                          int64_t nsteps, double dt, double eps, int precision, double* xbar, double* vbar,
+                          double* mbar, cudaStream_t st) {
+  const unsigned b3 = (unsigned)((3 * n + 255) / 256);
+  for (int64_t j = nsteps - 1; j >= 0; j--) {
+    adj_pre_kernel<<<b3, 256, 0, st>>>(sx + 3 * n * j, sv + 3 * n * j, n, dt, xbar, vbar, (double*)ws.xh.ptr,
+                                       (double*)ws.w.ptr, (double*)ws.lam.ptr);
+    GH_LAUNCH_CHECK();
+    GH_TRY(direct_vjp((const double*)ws.xh.ptr, mass, n, eps, (const double*)ws.lam.ptr, precision,
+                      (double*)ws.gpos.ptr, (double*)ws.gmass.ptr, st));
+    adj_post_kernel<<<b3, 256, 0, st>>>(n, dt, (const double*)ws.w.ptr, (const double*)ws.gpos.ptr,
+                                        (const double*)ws.gmass.ptr, xbar, vbar, mbar);
+    GH_LAUNCH_CHECK();
+  }
+  return GH_OK;
+}
 
 int dkd_backward(const double* x0, const double* v0, const double* mass, int64_t n, int64_t nsteps, double dt,
                  double eps, int precision, double* xbar, double* vbar, double* mbar, cudaStream_t st) {
@@ -491,16 +513,75 @@ int dkd_backward(const double* x0, const double* v0, const double* mass, int64_t
     GH_TRY(direct_run((double*)ws.work_x.ptr, (double*)ws.work_v.ptr, mass, n, nsteps - 1, dt, eps, precision,
                       sx + 3 * n, sv + 3 * n, 1, st));
   }
-  const unsigned b3 = (unsigned)((3 * n + 255) / 256);
-  for (int64_t j = nsteps - 1; j >= 0; j--) {
-    adj_pre_kernel<<<b3, 256, 0, st>>>(sx + 3 * n * j, sv + 3 * n * j, n, dt, xbar, vbar, (double*)ws.xh.ptr,
-                                       (double*)ws.w.ptr, (double*)ws.lam.ptr);
-    GH_LAUNCH_CHECK();
-    GH_TRY(direct_vjp((const double*)ws.xh.ptr, mass, n, eps, (const double*)ws.lam.ptr, precision,
-                      (double*)ws.gpos.ptr, (double*)ws.gmass.ptr, st));
-    adj_post_kernel<<<b3, 256, 0, st>>>(n, dt, (const double*)ws.w.ptr, (const double*)ws.gpos.ptr,
-                                        (const double*)ws.gmass.ptr, xbar, vbar, mbar);
-    GH_LAUNCH_CHECK();
+  return backward_steps(ws, sx, sv, mass, n, nsteps, dt, eps, precision, xbar, vbar, mbar, st);
+}
+
+// Multi-segment form: the checkpoints of all segments at once; segment s-1 is
+// recomputed on a second stream while segment s back-propagates on `st` (two state
+// buffers, ordered by events), so the recomputation overlaps the VJP launches.
+int dkd_backward_chain(const double* cx, const double* cv, const int64_t* seg, int64_t nseg, const double* mass,
+                       int64_t n, double dt, double eps, int precision, double* xbar, double* vbar, double* mbar,
+                       cudaStream_t st) {
+  if (n < 0 || nseg < 0) return set_error(GH_ERR_ARG, "negative n or segment count");
+  if (n == 0 || nseg == 0) return GH_OK;
+  if (!cx || !cv || !seg || !mass || !xbar || !vbar) return set_error(GH_ERR_ARG, "null buffer");
+  int64_t maxseg = 0;
+  for (int64_t s = 0; s < nseg; s++) {
+    if (seg[s] < 1) return set_error(GH_ERR_ARG, "segment %lld has %lld steps", (long long)s, (long long)seg[s]);
+    if (seg[s] > maxseg) maxseg = seg[s];
+  }
+  std::lock_guard<std::mutex> lk(g_bwd_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  BwdWS& ws = g_bwd[di.device];
+  const size_t vec = (size_t)n * 3 * sizeof(double);
+  for (int b = 0; b < 2; b++) {
+    GH_TRY(ensure(ws.chain_x[b], vec * maxseg));
+    GH_TRY(ensure(ws.chain_v[b], vec * maxseg));
+  }
+  GH_TRY(ensure(ws.work_x, vec));
+  GH_TRY(ensure(ws.work_v, vec));
+  GH_TRY(ensure(ws.xh, vec));
+  GH_TRY(ensure(ws.w, vec));
+  GH_TRY(ensure(ws.lam, vec));
+  GH_TRY(ensure(ws.gpos, vec));
+  GH_TRY(ensure(ws.gmass, (size_t)n * sizeof(double)));
+  if (!ws.rstream) {
+    GH_CUDA_TRY(cudaStreamCreateWithFlags(&ws.rstream, cudaStreamNonBlocking));
+    for (int b = 0; b < 3; b++) GH_CUDA_TRY(cudaEventCreateWithFlags(&ws.ev[b], cudaEventDisableTiming));
+  }
+  cudaStream_t rs = ws.rstream;
+  cudaEvent_t ev_ready[2] = {ws.ev[0], ws.ev[1]};  // recomputed segment in buffer b
+  cudaEvent_t ev_free = ws.ev[2];                  // the backward that last read a buffer
+  GH_CUDA_TRY(cudaEventRecord(ev_free, st));        // the caller's work before anything here
+  GH_CUDA_TRY(cudaStreamWaitEvent(rs, ev_free, 0));
+  auto recompute = [&](int64_t s) -> int {
+    const int b = (int)(s & 1);
+    double* sx = (double*)ws.chain_x[b].ptr;
+    double* sv = (double*)ws.chain_v[b].ptr;
+    GH_CUDA_TRY(cudaMemcpyAsync(sx, cx + 3 * n * s, vec, cudaMemcpyDeviceToDevice, rs));
+    GH_CUDA_TRY(cudaMemcpyAsync(sv, cv + 3 * n * s, vec, cudaMemcpyDeviceToDevice, rs));
+    if (seg[s] > 1) {
+      GH_CUDA_TRY(cudaMemcpyAsync(ws.work_x.ptr, cx + 3 * n * s, vec, cudaMemcpyDeviceToDevice, rs));
+      GH_CUDA_TRY(cudaMemcpyAsync(ws.work_v.ptr, cv + 3 * n * s, vec, cudaMemcpyDeviceToDevice, rs));
+      GH_TRY(direct_run((double*)ws.work_x.ptr, (double*)ws.work_v.ptr, mass, n, seg[s] - 1, dt, eps, precision,
+                        sx + 3 * n, sv + 3 * n, 1, rs));
+    }
+    GH_CUDA_TRY(cudaEventRecord(ev_ready[b], rs));
+    return GH_OK;
+  };
+  GH_TRY(recompute(nseg - 1));
+  for (int64_t s = nseg - 1; s >= 0; s--) {
+    const int b = (int)(s & 1);
+    GH_CUDA_TRY(cudaStreamWaitEvent(st, ev_ready[b], 0));
+    if (s >= 1) {
+      // buffer (s-1)&1 was last read by the backward of segment s+1
+      if (s + 1 < nseg) GH_CUDA_TRY(cudaStreamWaitEvent(rs, ev_free, 0));
+      GH_TRY(recompute(s - 1));
+    }
+    GH_TRY(backward_steps(ws, (const double*)ws.chain_x[b].ptr, (const double*)ws.chain_v[b].ptr, mass, n, seg[s],
+                          dt, eps, precision, xbar, vbar, mbar, st));
+    GH_CUDA_TRY(cudaEventRecord(ev_free, st));
   }
   return GH_OK;
 }

@@ -171,6 +171,17 @@ int gh_dkd_backward_dev(const double* x0, const double* v0, const double* mass, 
   return dkd_backward(x0, v0, mass, np, nsteps, dt, eps, precision, xbar, vbar, mbar, (cudaStream_t)stream);
 }
 
+int gh_dkd_backward_chain_dev(const double* ckpt_x, const double* ckpt_v, const int64_t* seg_steps, int64_t nseg,
+                              const double* mass, int64_t np, double dt, double eps, int precision, double* xbar,
+                              double* vbar, double* mbar, void* stream) {
+  clear_error();
+  if (precision != GH_PREC_FP64 && precision != GH_PREC_MIXED)
+    return set_error(GH_ERR_ARG, "unknown precision %d", precision);
+  if (!(eps >= 0.0)) return set_error(GH_ERR_ARG, "eps must be >= 0");
+  return dkd_backward_chain(ckpt_x, ckpt_v, seg_steps, nseg, mass, np, dt, eps, precision, xbar, vbar, mbar,
+                            (cudaStream_t)stream);
+}
+
 int gh_potential_dev(const double* pos, const double* mass, int64_t np, double eps, double* phi, void* stream) {
   clear_error();
   return potential(pos, mass, np, eps, phi, (cudaStream_t)stream);

@@ -41,6 +41,9 @@ int direct_vjp(const double* pos, const double* mass, int64_t n, double eps, con
 // states, then updates the cotangents (xbar, vbar) in place and adds to mbar.
 int dkd_backward(const double* x0, const double* v0, const double* mass, int64_t n, int64_t nsteps, double dt,
                  double eps, int precision, double* xbar, double* vbar, double* mbar, cudaStream_t st);
+int dkd_backward_chain(const double* cx, const double* cv, const int64_t* seg, int64_t nseg, const double* mass,
+                       int64_t n, double dt, double eps, int precision, double* xbar, double* vbar, double* mbar,
+                       cudaStream_t st);
 
 // Per-particle softened potential phi_k = -sum_{j != k} m_j / sqrt(r^2 + eps^2) (G=1).
 int potential(const double* pos, const double* mass, int64_t n, double eps, double* phi, cudaStream_t st);

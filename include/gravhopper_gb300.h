@@ -146,6 +146,14 @@ int gh_direct_vjp_dev(const double* pos, const double* mass, int64_t np, double 
  * cotangents of the state after the last step, on return those of (x0, v0); mbar,
  * when non-NULL, is incremented by the mass gradient.  One checkpoint segment of a
  * differentiable rollout. */
+/* The same for a whole checkpointed rollout: ckpt_x, ckpt_v (nseg,np,3) hold the state
+ * at the start of each segment, seg_steps (host array, nseg entries) the segments'
+ * step counts.  The segments are taken in reverse; each one's states are recomputed
+ * on a second stream while the following segment back-propagates on `stream`. */
+int gh_dkd_backward_chain_dev(const double* ckpt_x, const double* ckpt_v, const int64_t* seg_steps, int64_t nseg,
+                              const double* mass, int64_t np, double dt, double eps, int precision, double* xbar,
+                              double* vbar, double* mbar, void* stream);
+
 int gh_dkd_backward_dev(const double* x0, const double* v0, const double* mass, int64_t np, int64_t nsteps,
                         double dt, double eps, int precision, double* xbar, double* vbar, double* mbar,
                         void* stream);
