@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--cpu-targets", type=int, default=49152,
                     help="targets in the CPU-baseline sample (each against all N sources)")
-    ap.add_argument("--report", choices=["config0", "config1", "config4"],
+    ap.add_argument("--report", choices=["config0", "config1", "config2", "config4"],
                     help="print one JSON line of the full measurements for that workload instead")
     return ap.parse_args()
 
@@ -170,7 +170,8 @@ def main():
         import torch
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(0)
-        fn = {"config0": report_config0, "config1": report_config1, "config4": report_config4}[args.report]
+        fn = {"config0": report_config0, "config1": report_config1, "config2": report_config2,
+              "config4": report_config4}[args.report]
         print(json.dumps({"report": args.report, **fn(dev)}), flush=True)
         return
     import numpy as np
@@ -532,6 +533,39 @@ def report_config1(dev):
             row[prec] = r
         row["mixed_over_fp64"] = row["mixed"]["gpair_s"] / row["fp64"]["gpair_s"]
         out[f"n_{n}"] = row
+    return out
+
+
+def report_config2(dev, n=1 << 20, steps=100):
+    """Hernquist + exponential disk, N = 1,048,576: 100 DKD steps through
+    Simulation.run with the tree at theta 0.7 and 0.5 (mixed and FP64 walks), and the
+    force's error against the oracle tree (the reference's algorithm) on 2048 sampled
+    targets of the initial state."""
+    import numpy as np
+    import torch
+
+    import gravhopper_gb300 as gh
+    from gravhopper_gb300 import engine, ics
+    from oracle import oracle
+    ic = ics.hernquist_disk(n, seed=1)
+    rng = np.random.default_rng(4)
+    idx = rng.choice(n, size=2048, replace=False)
+    x = torch.from_numpy(ic["pos"]).to(dev)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    out = {"n": n, "steps": steps}
+    for theta in (0.7, 0.5):
+        ref = oracle.tree_force_position(ic["pos"], ic["mass"], ic["pos"][idx], 0.1, theta)
+        row = {}
+        for prec in ("mixed", "fp64"):
+            got = engine.tree_force(x, m, 0.1, theta, force_pos=x[torch.from_numpy(idx).to(dev)].contiguous(),
+                                    precision=prec).cpu().numpy()
+            r = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+            sim = gh.Simulation(dt=0.5, eps=0.1, algorithm="tree", theta=theta, precision=prec)
+            sim.add_IC(ic)
+            t = _timed(lambda: sim.run(steps))
+            row[prec] = {"run_s": t, "particle_steps_per_s": n * steps / t, "rel_err_rms": float(np.sqrt(np.mean(r * r))),
+                         "rel_err_max": float(r.max())}
+        out[f"theta_{theta}"] = row
     return out
 
 
