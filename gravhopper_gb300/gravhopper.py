@@ -198,8 +198,9 @@ class Simulation(object):
                               precision=self.params["precision"], theta=self.params["theta"],
                               hist_stride=1)
         hp, hv = hist
-        self._pos[t0 + 1:t0 + N + 1] = hp.cpu().numpy()
-        self._vel[t0 + 1:t0 + N + 1] = hv.cpu().numpy()
+        # copy straight into the history arrays (one device -> host copy each)
+        torch.from_numpy(self._pos[t0 + 1:t0 + N + 1]).copy_(hp)
+        torch.from_numpy(self._vel[t0 + 1:t0 + N + 1]).copy_(hv)
         dt = self._dt()
         for k in range(t0 + 1, t0 + N + 1):
             self._times[k] = self._times[k - 1] + dt
