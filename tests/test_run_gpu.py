@@ -49,7 +49,7 @@ def test_mixed_run_energy_drift(golden, lib, cuda):
     """The leapfrog at dt = 0.005 Myr does not conserve energy for this sphere: the
     reference's own FP64 trajectory drifts by 15.6 % over 400 steps, and a 1e-12
     perturbation of the initial positions changes the step-400 energy by 5.6e-3
-    (chaos).  So precision is judged (a) early, before chaos amplifies differences,
+    (chaos).  So precision is assessed (a) early, before chaos amplifies differences,
     against the FP64 trajectory, and (b) on the same sphere at dt = 5e-5 Myr, where
     the FP64 integration drifts by only ~1e-8: there the mixed run must stay within
     the 1e-5 relative energy drift target over 400 steps."""
