@@ -51,7 +51,7 @@ def parse():
     ap.add_argument("--no-secondary", action="store_true")
     ap.add_argument("--cpu-targets", type=int, default=49152,
                     help="targets in the CPU-baseline sample (each against all N sources)")
-    ap.add_argument("--report", choices=["config0", "config1", "config2", "config4"],
+    ap.add_argument("--report", choices=["config0", "config1", "config2", "config3", "config4"],
                     help="print one JSON line of the full measurements for that workload instead")
     return ap.parse_args()
 
@@ -171,7 +171,7 @@ def main():
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(0)
         fn = {"config0": report_config0, "config1": report_config1, "config2": report_config2,
-              "config4": report_config4}[args.report]
+              "config3": report_config3, "config4": report_config4}[args.report]
         print(json.dumps({"report": args.report, **fn(dev)}), flush=True)
         return
     import numpy as np
@@ -567,6 +567,41 @@ def report_config2(dev, n=1 << 20, steps=100):
                          "rel_err_max": float(r.max())}
         out[f"theta_{theta}"] = row
     return out
+
+
+def report_config3(dev, steps=1000, loop_steps=20):
+    """512 Plummer spheres (N log-uniform in [256, 8192], b in [0.5, 2] pc, eps = 0.05 b,
+    dt = 0.005 Myr (b / pc)^1.5): 1000 mixed steps in one persistent launch per step from
+    a CUDA graph with the autotuned tiles, against integrating the systems one by one;
+    relative energy drift of every system (FP64 energies)."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    from gravhopper_gb300.ensemble import Ensemble, autotune, run_one_by_one
+    systems = ics.plummer_ensemble(512, seed=0)
+    e = Ensemble(systems, device=dev)
+
+    def energies(ens):
+        out = []
+        for k in range(ens.nsys):
+            a, b = int(ens.offsets[k]), int(ens.offsets[k + 1])
+            out.append(engine.energy(ens.pos[a:b].contiguous(), ens.vel[a:b].contiguous(),
+                                     ens.mass[a:b].contiguous(), float(ens.eps[k]))[2])
+        return np.array(out)
+
+    best, _ = autotune(e, steps=4, use_cache=False)
+    e0 = energies(e)
+    t = _timed(lambda: e.run(steps, use_graph=True))
+    drift = np.abs(energies(e) - e0) / np.abs(e0)
+    f = Ensemble(systems, device=dev)
+    run_one_by_one(f, 1)
+    tl = _timed(lambda: run_one_by_one(f, loop_steps))
+    pairs = e.pairs_per_step
+    return {"systems": e.nsys, "particles": int(e.offsets[-1]), "steps": steps, "tile_config": best,
+            "run_s": t, "ms_per_step": t / steps * 1e3, "gpair_s": pairs * steps / t / 1e9,
+            "one_by_one_ms_per_step": tl / loop_steps * 1e3, "speedup_vs_one_by_one": (tl / loop_steps) / (t / steps),
+            "energy_drift_median": float(np.median(drift)), "energy_drift_max": float(drift.max())}
 
 
 def report_config4(dev, n=16384):
