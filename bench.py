@@ -597,11 +597,24 @@ def report_config3(dev, steps=1000, loop_steps=20):
     f = Ensemble(systems, device=dev)
     run_one_by_one(f, 1)
     tl = _timed(lambda: run_one_by_one(f, loop_steps))
+    # the same drift measured on 16 of the systems integrated alone in FP64
+    sample = np.linspace(0, e.nsys - 1, 16).astype(int)
+    d64 = []
+    for k in sample:
+        sysk = systems[int(k)]
+        x = torch.from_numpy(np.ascontiguousarray(sysk["pos"])).to(dev)
+        v = torch.from_numpy(np.ascontiguousarray(sysk["vel"])).to(dev)
+        m = torch.from_numpy(np.ascontiguousarray(sysk["mass"])).to(dev)
+        ea = engine.energy(x, v, m, float(sysk["eps"]))[2]
+        engine.run_dkd(x, v, m, steps, float(sysk["dt"]), float(sysk["eps"]), precision="fp64")
+        d64.append(abs(engine.energy(x, v, m, float(sysk["eps"]))[2] - ea) / abs(ea))
     pairs = e.pairs_per_step
     return {"systems": e.nsys, "particles": int(e.offsets[-1]), "steps": steps, "tile_config": best,
             "run_s": t, "ms_per_step": t / steps * 1e3, "gpair_s": pairs * steps / t / 1e9,
             "one_by_one_ms_per_step": tl / loop_steps * 1e3, "speedup_vs_one_by_one": (tl / loop_steps) / (t / steps),
-            "energy_drift_median": float(np.median(drift)), "energy_drift_max": float(drift.max())}
+            "energy_drift_median": float(np.median(drift)), "energy_drift_max": float(drift.max()),
+            "sample_systems": [int(k) for k in sample],
+            "sample_drift_ensemble": [float(drift[k]) for k in sample], "sample_drift_fp64_alone": d64}
 
 
 def report_config4(dev, n=16384):
