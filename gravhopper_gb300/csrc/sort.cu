@@ -1,9 +1,9 @@
 // Stable LSD radix sort (8-bit digits, multi-word keys) and exclusive scan.
 //
 // Each sort pass is one launch (one-sweep, below) after one histogram launch per
-// key word.  Stability inside a tile comes from processing the tile in rounds of one
-// item per thread (item order = round, then thread) and ranking equal digits within a
-// warp with __match_any_sync, across warps with a per-round prefix over the warp
+// key word.  Stability inside a tile comes from giving each warp a contiguous block of
+// the tile's items, ranked in order within the warp (match-any per round of 32 items,
+// a warp-local running count per digit) and across warps by a prefix over the warps'
 // counts; across tiles from the tiles' ticket order.
 #include "sort.cuh"
 
@@ -108,29 +108,31 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
                    uint32_t* __restrict__ iout, int words, int64_t n, int w, int shift,
                    const uint32_t* __restrict__ doff, uint32_t* __restrict__ status, int* __restrict__ ticket,
                    int* __restrict__ err) {
+  // Blocked layout: warp wi owns the tile's items [wi*256, wi*256+256), lane l of it
+  // item wi*256 + r*32 + l in round r.  A warp ranks its items by itself (match-any per
+  // round and a warp-local running count per digit); one prefix over the warps per
+  // digit then gives every item its place, so the tile needs two barriers.
   constexpr int NW = RS_THREADS / 32;
+  constexpr int WITEMS = 32 * RS_ROUNDS;  // items per warp
   __shared__ uint32_t warp_cnt[NW][RS_BINS];
-  __shared__ uint32_t warp_off[NW][RS_BINS];
   __shared__ uint32_t cursor[RS_BINS];
-  __shared__ uint32_t round_tot[RS_BINS];
-  __shared__ uint32_t tile_cnt[RS_BINS];
   __shared__ int s_tile;
   static_assert(RS_THREADS == RS_BINS, "one digit bin per thread");
-  const int tid = threadIdx.x, warp = tid >> 5;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   if (tid == 0) s_tile = atomicAdd(ticket, 1);
-  tile_cnt[tid] = 0;
 #pragma unroll
   for (int k = 0; k < NW; k++) warp_cnt[k][tid] = 0;
   __syncthreads();
   const int tile = s_tile;
-  const int64_t base = (int64_t)tile * RS_TILE;
+  const int64_t base = (int64_t)tile * RS_TILE + (int64_t)warp * WITEMS + lane;
   const uint64_t* kw = kin + (int64_t)w * n;
   unsigned dig[RS_ROUNDS];
+  uint32_t rank[RS_ROUNDS];
   uint64_t kr[RS_ROUNDS][WK > 0 ? WK : 1];
   uint32_t ir[RS_ROUNDS];
 #pragma unroll
   for (int r = 0; r < RS_ROUNDS; r++) {
-    const int64_t i = base + r * RS_THREADS + tid;
+    const int64_t i = base + r * 32;
     if (WK > 0) {
 #pragma unroll
       for (int q = 0; q < (WK > 0 ? WK : 1); q++) kr[r][q] = i < n ? kin[(int64_t)q * n + i] : 0ull;
@@ -139,17 +141,30 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
       kr[r][0] = i < n ? kw[i] : 0ull;
     }
   }
+  uint32_t* wc = warp_cnt[warp];
 #pragma unroll
   for (int r = 0; r < RS_ROUNDS; r++) {
-    const int64_t i = base + r * RS_THREADS + tid;
+    const int64_t i = base + r * 32;
     const uint64_t kd = (WK == 2 && w == 1) ? kr[r][WK > 1 ? 1 : 0] : kr[r][0];  // no dynamic register index
     dig[r] = i < n ? (unsigned)((kd >> shift) & 255u) : 256u;
     const unsigned peers = __match_any_sync(0xffffffffu, dig[r]);
-    if (dig[r] < 256u && (peers & lanemask_lt()) == 0) atomicAdd(&tile_cnt[dig[r]], (uint32_t)__popc(peers));
+    const unsigned below = __popc(peers & lanemask_lt());
+    const bool valid = dig[r] < 256u;
+    rank[r] = (valid ? wc[dig[r]] : 0u) + below;  // earlier rounds' count, then earlier lanes
+    __syncwarp();
+    if (valid && below == 0) wc[dig[r]] += (uint32_t)__popc(peers);
+    __syncwarp();
   }
   __syncthreads();
+  // thread tid = digit: its count in the tile, and each warp's offset within the tile
+  uint32_t cnt = 0;
+#pragma unroll
+  for (int k = 0; k < NW; k++) {
+    const uint32_t c = warp_cnt[k][tid];
+    warp_cnt[k][tid] = cnt;  // now the warp's offset for this digit
+    cnt += c;
+  }
   // publish this tile's count of digit tid, then add up the earlier tiles' counts
-  const uint32_t cnt = tile_cnt[tid];
   uint32_t excl = 0;
   uint32_t* my = status + (int64_t)tile * RS_BINS + tid;
   if (tile == 0) {
@@ -182,30 +197,12 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
   }
   cursor[tid] = doff[tid] + excl;
   __syncthreads();
-  // stable ranks in item order: rounds of one item per thread, warps in order
 #pragma unroll
   for (int r = 0; r < RS_ROUNDS; r++) {
-    const int64_t i = base + r * RS_THREADS + tid;
-    const bool valid = i < n;
-    const unsigned d = dig[r];
-    const unsigned peers = __match_any_sync(0xffffffffu, d);
-    const unsigned rank = __popc(peers & lanemask_lt());
-    if (valid && rank == 0) warp_cnt[warp][d] = __popc(peers);
-    __syncthreads();
-    {
-      uint32_t run = 0;
-#pragma unroll
-      for (int k = 0; k < NW; k++) {
-        const uint32_t c = warp_cnt[k][tid];
-        warp_off[k][tid] = run;
-        run += c;
-        warp_cnt[k][tid] = 0;
-      }
-      round_tot[tid] = run;
-    }
-    __syncthreads();
-    if (valid) {
-      const int64_t pos = (int64_t)cursor[d] + warp_off[warp][d] + rank;
+    const int64_t i = base + r * 32;
+    if (i < n) {
+      const unsigned d = dig[r];
+      const int64_t pos = (int64_t)cursor[d] + wc[d] + rank[r];
       if (WK > 0) {
 #pragma unroll
         for (int q = 0; q < (WK > 0 ? WK : 1); q++) kout[(int64_t)q * n + pos] = kr[r][q];
@@ -215,9 +212,6 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
         iout[pos] = iin[i];
       }
     }
-    __syncthreads();
-    cursor[tid] += round_tot[tid];
-    __syncthreads();
   }
 }
 
