@@ -53,6 +53,7 @@ _lib = None
 _lock = threading.Lock()
 
 _i64 = ctypes.c_int64
+_u64 = ctypes.c_uint64
 _dbl = ctypes.c_double
 _int = ctypes.c_int
 _vp = ctypes.c_void_p
@@ -85,6 +86,7 @@ SIGNATURES = {
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),
     "gh_measure_l2_read": (_int, [_vp, _vp]),
+    "gh_check_inv_cube": (_int, [_i64, _u64, _vp, _vp]),
     "gh_tree_stats": (_int, [_int]),
     "gh_tree_stats_read": (_int, [_vp]),
 }
@@ -169,6 +171,14 @@ def measure_l2_read(stream=None):
     b = ctypes.c_double(0.0)
     call("gh_measure_l2_read", ctypes.addressof(b), stream_handle(stream))
     return b.value
+
+
+def check_inv_cube(n: int, seed: int = 1, stream=None):
+    """(wrong, fallback): integer-pipe inverse cube against the native IEEE operations
+    on n seeded inputs on the current device."""
+    out = (ctypes.c_longlong * 2)()
+    call("gh_check_inv_cube", int(n), int(seed), ctypes.addressof(out), stream_handle(stream))
+    return int(out[0]), int(out[1])
 
 
 def tree_stats(enable: bool) -> None:

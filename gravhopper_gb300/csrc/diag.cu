@@ -1,6 +1,7 @@
 // Throughput probes used as roofline denominators, timed with CUDA events on the
 // current device: FP32 FMA (f32x2 packed) and FP64 FMA lane-operations per second,
-// and the L2 read bandwidth for a buffer that stays resident in L2.
+// and the L2 read bandwidth for a buffer that stays resident in L2; and a self-check
+// of the integer-pipe FP64 inverse cube against the native IEEE operations.
 #include "direct.cuh"
 #include "gh_common.cuh"
 
@@ -128,7 +129,76 @@ static int time_l2(int64_t bytes, int reps, cudaStream_t st, double* bytes_per_s
   return GH_OK;
 }
 
+// Self-check of the integer-pipe inverse cube (f64emu.cuh) on this device: n seeded
+// inputs, half with uniform significand and exponent over [2^-723, 2^727), half of
+// the form dx^2 + dy^2 + dz^2 + eps^2 met by the direct sum, each compared bit for
+// bit with the native RN(RN(1/s) / RN(sqrt(s))).
+__device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
+  x += 0x9E3779B97F4A7C15ull;
+  x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+  x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+  return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double unit_from(uint64_t r) { return (double)(r >> 11) * 0x1p-53; }
+
+__global__ void __launch_bounds__(256)
+    inv_cube_check_kernel(int64_t n, uint64_t seed, unsigned long long* counts) {
+  unsigned long long wrong = 0, fallback = 0;
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t r0 = splitmix64(seed + 2 * (uint64_t)i), r1 = splitmix64(seed + 2 * (uint64_t)i + 1);
+    double s;
+    if (i & 1) {
+      s = __longlong_as_double(
+          (long long)((r0 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(300 + (r1 >> 52) % 1450) << 52)));
+    } else {
+      const double dx = ldexp(unit_from(r0) - 0.5, -(int)(r1 & 31));
+      const double dy = ldexp(unit_from(r1) - 0.5, -(int)((r0 >> 5) & 31));
+      const double dz = unit_from(r0 ^ r1) * 0x1p-7;
+      const double eps = 5e-5 * (double)(r1 % 3);
+      s = dadd(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), dmul(eps, eps));
+    }
+    const double want = ddiv(ddiv(1.0, s), dsqrt(s));
+    double got;
+    const int E = (int)((uint64_t)__double_as_longlong(s) >> 52);
+    if (emu::inv_cube_rn(s, got)) {
+      wrong += __double_as_longlong(got) != __double_as_longlong(want);
+    } else {
+      fallback += E >= 446 && E <= 1624;
+    }
+  }
+  for (int o = 16; o; o >>= 1) {
+    wrong += __shfl_xor_sync(0xffffffffu, wrong, o);
+    fallback += __shfl_xor_sync(0xffffffffu, fallback, o);
+  }
+  if ((threadIdx.x & 31) == 0 && (wrong || fallback)) {
+    atomicAdd(&counts[0], wrong);
+    atomicAdd(&counts[1], fallback);
+  }
+}
+
 }  // namespace gh
+
+extern "C" int gh_check_inv_cube(int64_t n, uint64_t seed, long long* wrong_fallback, void* stream) {
+  using namespace gh;
+  clear_error();
+  if (!wrong_fallback || n < 0) return set_error(GH_ERR_ARG, "inverse-cube check: bad arguments");
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  const cudaStream_t st = (cudaStream_t)stream;
+  static Buffer counts;
+  GH_TRY(ensure(counts, 2 * sizeof(unsigned long long)));
+  GH_CUDA_TRY(cudaMemsetAsync(counts.ptr, 0, 2 * sizeof(unsigned long long), st));
+  inv_cube_check_kernel<<<4 * di.num_sms, 256, 0, st>>>(n, seed, (unsigned long long*)counts.ptr);
+  GH_LAUNCH_CHECK();
+  unsigned long long h[2];
+  GH_CUDA_TRY(cudaMemcpyAsync(h, counts.ptr, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GH_CUDA_TRY(cudaStreamSynchronize(st));
+  wrong_fallback[0] = (long long)h[0];
+  wrong_fallback[1] = (long long)h[1];
+  return GH_OK;
+}
 
 extern "C" int gh_measure_l2_read(double* bytes_per_s, void* stream) {
   using namespace gh;

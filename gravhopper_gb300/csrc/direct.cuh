@@ -4,6 +4,7 @@
 #pragma once
 
 #include "gh_common.cuh"
+#include "f64emu.cuh"
 
 namespace gh {
 
@@ -175,8 +176,8 @@ __global__ void __launch_bounds__(F64_THREADS)
         r2 = dadd(r2, dmul(dy, dy));
         r2 = dadd(r2, dmul(dz, dz));
         double ss = dadd(r2, eps2);
-        double inv = ddiv(ddiv(1.0, ss), dsqrt(ss));
-        if (!SELF && ss == 0.0) inv = 0.0;
+        double inv;
+        if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
         ax[r] = dadd(ax[r], dmul(dmul(s.w, dx), inv));
         ay[r] = dadd(ay[r], dmul(dmul(s.w, dy), inv));
         az[r] = dadd(az[r], dmul(dmul(s.w, dz), inv));
@@ -234,8 +235,8 @@ __global__ void __launch_bounds__(F64O_THREADS)
         r2 = dadd(r2, dmul(dy, dy));
         r2 = dadd(r2, dmul(dz, dz));
         const double ss = dadd(r2, eps2);
-        double inv = ddiv(ddiv(1.0, ss), dsqrt(ss));
-        if (!SELF && ss == 0.0) inv = 0.0;
+        double inv;
+        if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
         vx = dmul(dmul(s.w, dx), inv);
         vy = dmul(dmul(s.w, dy), inv);
         vz = dmul(dmul(s.w, dz), inv);
