@@ -132,7 +132,8 @@ static int time_l2(int64_t bytes, int reps, cudaStream_t st, double* bytes_per_s
 // Self-check of the integer-pipe inverse cube (f64emu.cuh) on this device: n seeded
 // inputs, half with uniform significand and exponent over [2^-723, 2^727), half of
 // the form dx^2 + dy^2 + dz^2 + eps^2 met by the direct sum, each compared bit for
-// bit with the native RN(RN(1/s) / RN(sqrt(s))).
+// bit with the native RN(RN(1/s) / RN(sqrt(s))); the second half also through the
+// integer-pipe squared distance (pair_inv_cube_rn from the signed components).
 __device__ __forceinline__ uint64_t splitmix64(uint64_t x) {
   x += 0x9E3779B97F4A7C15ull;
   x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
@@ -148,7 +149,7 @@ __global__ void __launch_bounds__(256)
   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t r0 = splitmix64(seed + 2 * (uint64_t)i), r1 = splitmix64(seed + 2 * (uint64_t)i + 1);
-    double s;
+    double s, pair_d[3] = {0.0, 0.0, 0.0}, pair_eps2 = 0.0;
     if (i & 1) {
       s = __longlong_as_double(
           (long long)((r0 & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(300 + (r1 >> 52) % 1450) << 52)));
@@ -157,7 +158,11 @@ __global__ void __launch_bounds__(256)
       const double dy = ldexp(unit_from(r1) - 0.5, -(int)((r0 >> 5) & 31));
       const double dz = unit_from(r0 ^ r1) * 0x1p-7;
       const double eps = 5e-5 * (double)(r1 % 3);
-      s = dadd(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), dmul(eps, eps));
+      pair_eps2 = dmul(eps, eps);
+      s = dadd(dadd(dadd(dmul(dx, dx), dmul(dy, dy)), dmul(dz, dz)), pair_eps2);
+      pair_d[0] = (r0 & 1) ? -dx : dx;
+      pair_d[1] = (r0 & 2) ? -dy : dy;
+      pair_d[2] = (r0 & 4) ? -dz : dz;
     }
     const double want = ddiv(ddiv(1.0, s), dsqrt(s));
     double got;
@@ -166,6 +171,15 @@ __global__ void __launch_bounds__(256)
       wrong += __double_as_longlong(got) != __double_as_longlong(want);
     } else {
       fallback += E >= 446 && E <= 1624;
+    }
+    if (!(i & 1)) {  // the same factor from the components, squared distance included
+      int eE;
+      uint64_t eM;
+      emu::unpack_eps2(pair_eps2, eE, eM);
+      if (emu::pair_inv_cube_rn(pair_d[0], pair_d[1], pair_d[2], eE, eM, got))
+        wrong += __double_as_longlong(got) != __double_as_longlong(want);
+      else
+        fallback += pair_d[0] != 0.0 && pair_d[1] != 0.0 && pair_d[2] != 0.0;
     }
   }
   for (int o = 16; o; o >>= 1) {

@@ -147,6 +147,9 @@ __global__ void __launch_bounds__(F64_THREADS)
   const int64_t base = (int64_t)blockIdx.x * (F64_THREADS * F64_R) + threadIdx.x;
   double tx[F64_R], ty[F64_R], tz[F64_R], ax[F64_R], ay[F64_R], az[F64_R];
   int64_t ti[F64_R];
+  int e2E;
+  uint64_t e2M;
+  const bool emu_ok = emu::unpack_eps2(eps2, e2E, e2M);  // integer-pipe pair factor usable
 #pragma unroll
   for (int r = 0; r < F64_R; r++) {
     ti[r] = base + r * F64_THREADS;
@@ -172,12 +175,14 @@ __global__ void __launch_bounds__(F64_THREADS)
         double dx = dsub(s.x, tx[r]);
         double dy = dsub(s.y, ty[r]);
         double dz = dsub(s.z, tz[r]);
-        double r2 = dmul(dx, dx);
-        r2 = dadd(r2, dmul(dy, dy));
-        r2 = dadd(r2, dmul(dz, dz));
-        double ss = dadd(r2, eps2);
         double inv;
-        if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+        if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
+          double r2 = dmul(dx, dx);
+          r2 = dadd(r2, dmul(dy, dy));
+          r2 = dadd(r2, dmul(dz, dz));
+          const double ss = dadd(r2, eps2);
+          if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+        }
         ax[r] = dadd(ax[r], dmul(dmul(s.w, dx), inv));
         ay[r] = dadd(ay[r], dmul(dmul(s.w, dy), inv));
         az[r] = dadd(az[r], dmul(dmul(s.w, dz), inv));
@@ -214,6 +219,9 @@ __global__ void __launch_bounds__(F64O_THREADS)
     tp[tid / 3][tid % 3] = ti < nt ? tpos[3 * ti + tid % 3] : 0.0;
   }
   double sum = 0.0;  // threads < 3 TB: target tid / 3, component tid % 3
+  int e2E;
+  uint64_t e2M;
+  const bool emu_ok = emu::unpack_eps2(eps2, e2E, e2M);  // integer-pipe pair factor usable
   for (int64_t j0 = 0; j0 < np; j0 += F64O_JC) {
     __syncthreads();
     for (int k = tid; k < F64O_JC; k += F64O_THREADS) {
@@ -231,12 +239,14 @@ __global__ void __launch_bounds__(F64O_THREADS)
         const double dx = dsub(s.x, tp[t][0]);
         const double dy = dsub(s.y, tp[t][1]);
         const double dz = dsub(s.z, tp[t][2]);
-        double r2 = dmul(dx, dx);
-        r2 = dadd(r2, dmul(dy, dy));
-        r2 = dadd(r2, dmul(dz, dz));
-        const double ss = dadd(r2, eps2);
         double inv;
-        if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+        if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
+          double r2 = dmul(dx, dx);
+          r2 = dadd(r2, dmul(dy, dy));
+          r2 = dadd(r2, dmul(dz, dz));
+          const double ss = dadd(r2, eps2);
+          if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+        }
         vx = dmul(dmul(s.w, dx), inv);
         vy = dmul(dmul(s.w, dy), inv);
         vz = dmul(dmul(s.w, dz), inv);

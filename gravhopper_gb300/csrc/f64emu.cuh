@@ -105,13 +105,10 @@ GH_EMU_HD float rsqrt_seed(float x) {
 #endif
 }
 
-// RN(RN(1/s) / RN(sqrt(s))) into `out`; false when s is out of range or a check
-// fails (then `out` is untouched).
-GH_EMU_HD bool inv_cube_rn(double s, double& out) {
-  const uint64_t bits = dbits(s);
-  const int E = (int)(bits >> 52);  // biased exponent; the sign bit makes it >= 2048
-  if ((unsigned)(E - 446) > 1178u) return false;  // 2^-577 <= s < 2^602
-  const uint64_t M = (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+// RN(RN(1/s) / RN(sqrt(s))) into `out` for s = M 2^(E - 1075) with M in
+// [2^52, 2^53) and 446 <= E <= 1624 (the caller checks the range); false when a
+// check fails (then `out` is untouched).
+GH_EMU_HD bool inv_cube_core(int E, uint64_t M, double& out) {
   const int odd = ~E & 1;  // s = M 2^(E - 1075); E - 1075 is odd when E is even
   const uint64_t N = M << odd;  // s = N 2^p with p even, N in [2^52, 2^54)
   const int p = E - 1075 - odd;
@@ -190,6 +187,126 @@ GH_EMU_HD bool inv_cube_rn(double s, double& out) {
   const int k = sh - 54 + (970 - E) - (p / 2 - 26);
   out = bitsd(((uint64_t)(k + 1074) << 52) + m);  // m = 2^53 carries into the exponent
   return true;
+}
+
+// RN(RN(1/s) / RN(sqrt(s))) into `out`; false when s is out of range or a check
+// fails (then `out` is untouched).
+GH_EMU_HD bool inv_cube_rn(double s, double& out) {
+  const uint64_t bits = dbits(s);
+  const int E = (int)(bits >> 52);  // biased exponent; the sign bit makes it >= 2048
+  if ((unsigned)(E - 446) > 1178u) return false;  // 2^-577 <= s < 2^602
+  return inv_cube_core(E, (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull, out);
+}
+
+// ---------------------------------------------------------------------------
+// The softened squared distance s = RN(RN(RN(dx^2 + dy^2) + dz^2) + eps^2) with
+// every product and sum rounded as the FPU does (round to nearest even).  All terms
+// are positive, so a sum needs at most a one-bit renormalisation.  Values are
+// (E, M): M in [2^52, 2^53), value M 2^(E - 1075), E the biased exponent.
+
+// RN(d^2) of a normal d = D 2^(Ed - 1075); D^2 is formed exactly from 32-bit halves.
+GH_EMU_HD void square_rn(int Ed, uint64_t D, int& E, uint64_t& M) {
+  const uint32_t h = (uint32_t)(D >> 32), l = (uint32_t)D;  // h < 2^21
+  const uint64_t ll = (uint64_t)l * l;
+  const uint64_t x = (uint64_t)(2 * h) * l;  // < 2^54
+  const uint64_t lo = ll + (x << 32);
+  const uint64_t hi = (uint64_t)h * h + (x >> 32) + (lo < ll);  // D^2 = hi 2^64 + lo, hi in [2^40, 2^42)
+  const int big = (int)(hi >> 41);  // D^2 >= 2^105
+  uint64_t m;
+  uint64_t rest;  // the bits below m, left-aligned
+  if (big) {
+    m = (hi << 11) | (lo >> 53);
+    rest = lo << 11;
+  } else {
+    m = (hi << 12) | (lo >> 52);
+    rest = lo << 12;
+  }
+  m += (rest >> 63) & (uint64_t)(((rest << 1) != 0) | (m & 1));
+  E = 2 * Ed - 1023 + big;  // D^2 2^(2 Ed - 2150) = m 2^(52 + big + 2 Ed - 2150)
+  const int carry = (int)(m >> 53);
+  M = m >> carry;
+  E += carry;
+}
+
+// RN(a + b) of two positive normals.
+GH_EMU_HD void add_pos_rn(int Ea, uint64_t Ma, int Eb, uint64_t Mb, int& E, uint64_t& M) {
+  if (Ea < Eb) {
+    const int te = Ea;
+    Ea = Eb;
+    Eb = te;
+    const uint64_t tm = Ma;
+    Ma = Mb;
+    Mb = tm;
+  }
+  const int d = Ea - Eb;
+  if (d >= 54) {  // b < ulp(a) / 2
+    E = Ea;
+    M = Ma;
+    return;
+  }
+  const uint64_t bs = Mb << 10;
+  const uint64_t S = (Ma << 10) + (bs >> d);  // < 2^64
+  const bool lost = (bs & ((1ull << d) - 1)) != 0;
+  const int big = (int)(S >> 63);
+  uint64_t m, rest;
+  if (big) {
+    m = S >> 11;
+    rest = S << 53;
+  } else {
+    m = S >> 10;
+    rest = S << 54;
+  }
+  m += (rest >> 63) & (uint64_t)(((rest << 1) != 0) | lost | (m & 1));
+  const int carry = (int)(m >> 53);
+  M = m >> carry;
+  E = Ea + big + carry;
+}
+
+// Unpacks a double whose magnitude lies in [2^-250, 2^251) (zero excluded) into
+// (E, |significand|); false otherwise.
+GH_EMU_HD bool unpack_mid(double d, int& E, uint64_t& M) {
+  const uint64_t b = dbits(d);
+  E = (int)((b >> 52) & 0x7FF);
+  M = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  return (unsigned)(E - 773) <= 500u;
+}
+
+// Unpacks the squared softening for pair_inv_cube_rn: E = 0 for eps2 = 0; false
+// when eps2 lies outside [2^-500, 2^502) (then the caller uses the native path).
+GH_EMU_HD bool unpack_eps2(double eps2, int& E, uint64_t& M) {
+  const uint64_t b = dbits(eps2);
+  E = (int)(b >> 52);
+  M = (b & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull;
+  if (b == 0) {
+    E = 0;
+    return true;
+  }
+  return (unsigned)(E - 523) <= 1001u;
+}
+
+// inv = RN(RN(1/s) / RN(sqrt(s))) with s = RN(RN(RN(dx^2 + dy^2) + dz^2) + eps2),
+// the pair factor of gravhopper/_jbgrav.c:170-178.  eps2 is given unpacked
+// (eps2_E = 0 for eps2 = 0; otherwise 2^-500 <= eps2 < 2^502).  False when a
+// component is zero or outside [2^-250, 2^251), or a check fails.
+GH_EMU_HD bool pair_inv_cube_rn(double dx, double dy, double dz, int eps2_E, uint64_t eps2_M, double& out) {
+  int ex, ey, ez;
+  uint64_t mx, my, mz;
+  const bool ok = unpack_mid(dx, ex, mx) & unpack_mid(dy, ey, my) & unpack_mid(dz, ez, mz);
+  if (!ok) return false;
+  int E1, E2, E;
+  uint64_t M1, M2, M;
+  square_rn(ex, mx, E1, M1);
+  square_rn(ey, my, E2, M2);
+  add_pos_rn(E1, M1, E2, M2, E, M);
+  square_rn(ez, mz, E1, M1);
+  add_pos_rn(E, M, E1, M1, E2, M2);
+  if (eps2_E) {
+    add_pos_rn(E2, M2, eps2_E, eps2_M, E, M);
+  } else {
+    E = E2;
+    M = M2;
+  }
+  return inv_cube_core(E, M, out);
 }
 
 }  // namespace emu

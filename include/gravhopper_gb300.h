@@ -199,9 +199,11 @@ int gh_measure_l2_read(double* bytes_per_s, void* stream);
 
 /* Self-check of the integer-pipe softened inverse cube RN(RN(1/s)/RN(sqrt(s))) used
  * by the FP64 direct sum (no counterpart in the reference, whose C code evaluates
- * 1.0/s/sqrt(s) with the FPU, gravhopper/_jbgrav.c:176-178): n seeded inputs on the
- * current device compared bit for bit with the native IEEE operations.  Writes the
- * number of differing results and of in-range inputs that took the native path. */
+ * 1.0/s/sqrt(s) with the FPU, gravhopper/_jbgrav.c:170-178): n seeded inputs on the
+ * current device compared bit for bit with the native IEEE operations, half of them
+ * also through the integer-pipe squared distance s = dx^2 + dy^2 + dz^2 + eps^2.
+ * Writes the number of differing results and of in-range inputs that took the
+ * native path. */
 int gh_check_inv_cube(int64_t n, uint64_t seed, long long* wrong_fallback, void* stream);
 
 /* Enables (1) or disables (0) the tree-walk counters (no counterpart in the

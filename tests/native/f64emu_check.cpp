@@ -70,7 +70,7 @@ int main(int argc, char** argv) {
   const double special[] = {0.0, -0.0, -1.0, INFINITY, NAN, 4.9406564584124654e-324, 2.2250738585072014e-308,
                             1.7976931348623157e308};
   for (double s : special) check(s);
-  const long long per = cases / 4;
+  const long long per = cases / 5;
   // uniform significand and exponent over the fast range and beyond
   for (long long i = 0; i < per; i++) {
     const uint64_t b = (next_u64() & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(300 + next_u64() % 1450) << 52);
@@ -107,6 +107,63 @@ int main(int argc, char** argv) {
     const double dz = (double)(next_u64() >> 11) * 0x1p-60;
     const double eps = 5e-5 * (double)(next_u64() % 3);
     check(dx * dx + dy * dy + dz * dz + eps * eps);
+  }
+  // pair factors: s = ((dx^2 + dy^2) + dz^2) + eps2 and 1/s/sqrt(s), signed components
+  // often in one binade (ties in the sums), short significands (ties in the squares)
+  const double eps_list[] = {0.0, 5e-5, 1e-3, 0.1, 3.0};
+  for (long long i = 0; i < per; i++) {
+    double d[3];
+    const int e0 = (int)(next_u64() % 60) - 40;
+    for (int k = 0; k < 3; k++) {
+      const uint64_t r = next_u64();
+      int e = (r & 3) ? e0 : e0 - (int)(next_u64() % 60);
+      double sig;
+      if ((r >> 2) % 7 == 0)
+        sig = (double)((next_u64() >> 37) | 1) * 0x1p-27;  // short significand
+      else
+        sig = 1.0 + (double)(next_u64() >> 12) * 0x1p-52;
+      d[k] = ldexp((r >> 8) & 1 ? -sig : sig, e);
+    }
+    const double eps = eps_list[next_u64() % 5] * ((next_u64() & 1) ? 1.0 : 1.0 + (double)(next_u64() >> 40) * 0x1p-24);
+    const double eps2 = eps * eps;
+    const double ss = d[0] * d[0] + d[1] * d[1] + d[2] * d[2] + eps2;
+    const double want = 1.0 / ss / sqrt(ss);
+    int eE = 0;
+    uint64_t eM = 0;
+    if (eps2 != 0.0) gh::emu::unpack_mid(eps2, eE, eM);
+    double got = 0.0;
+    n_cases++;
+    if (gh::emu::pair_inv_cube_rn(d[0], d[1], d[2], eE, eM, got)) {
+      if (bits_of(got) != bits_of(want)) {
+        if (n_wrong < 10) printf("WRONG pair d=%.17g %.17g %.17g eps2=%.17g\n", d[0], d[1], d[2], eps2);
+        n_wrong++;
+      }
+    } else {
+      n_fallback++;
+    }
+    // the squared distance itself
+    int E1, E2, E;
+    uint64_t M1, M2, M;
+    int ex, ey, ez;
+    uint64_t mx, my, mz;
+    gh::emu::unpack_mid(d[0], ex, mx);
+    gh::emu::unpack_mid(d[1], ey, my);
+    gh::emu::unpack_mid(d[2], ez, mz);
+    gh::emu::square_rn(ex, mx, E1, M1);
+    gh::emu::square_rn(ey, my, E2, M2);
+    gh::emu::add_pos_rn(E1, M1, E2, M2, E, M);
+    const double s2 = d[0] * d[0] + d[1] * d[1];
+    const double s3 = s2 + d[2] * d[2];
+    if ((((uint64_t)(E - 1) << 52) + M) != bits_of(s2)) {
+      if (n_wrong < 10) printf("WRONG sum2 %.17g %.17g\n", d[0], d[1]);
+      n_wrong++;
+    }
+    gh::emu::square_rn(ez, mz, E1, M1);
+    gh::emu::add_pos_rn(E, M, E1, M1, E2, M2);
+    if ((((uint64_t)(E2 - 1) << 52) + M2) != bits_of(s3)) {
+      if (n_wrong < 10) printf("WRONG sum3 %.17g %.17g %.17g\n", d[0], d[1], d[2]);
+      n_wrong++;
+    }
   }
   printf("%lld %lld %lld %lld\n", n_cases, n_wrong, n_fallback, n_out);
   return n_wrong || n_out ? 1 : 0;

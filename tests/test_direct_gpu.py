@@ -118,10 +118,11 @@ def test_throughput_probes(lib, cuda):
 
 
 def test_integer_pipe_inverse_cube_matches_ieee(lib, cuda):
-    """The FP64 kernels evaluate RN(RN(1/s)/RN(sqrt(s))) on the integer pipes with the
-    device's FP32 rsqrt as seed; on 2^28 seeded inputs (uniform over 1450 binades and
-    r^2 + eps^2 sums) no confirmed result differs from the native IEEE operations and
-    no in-range input needs the native path."""
+    """The FP64 kernels evaluate s = dx^2 + dy^2 + dz^2 + eps^2 and
+    RN(RN(1/s)/RN(sqrt(s))) on the integer pipes with the device's FP32 rsqrt as seed;
+    on 2^28 seeded inputs (uniform over 1450 binades, and r^2 + eps^2 from signed
+    components) no confirmed result differs from the native IEEE operations and no
+    in-range input needs the native path."""
     from gravhopper_gb300 import _capi
     wrong, fallback = _capi.check_inv_cube(1 << 28, seed=7)
     assert wrong == 0
