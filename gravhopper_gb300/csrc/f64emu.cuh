@@ -105,13 +105,13 @@ GH_EMU_HD float rsqrt_seed(float x) {
 #endif
 }
 
-// RN(RN(1/s) / RN(sqrt(s))) into `out` for s = M 2^(E - 1075) with M in
-// [2^52, 2^53) and 446 <= E <= 1624 (the caller checks the range); false when a
-// check fails (then `out` is untouched).
-GH_EMU_HD bool inv_cube_core(int E, uint64_t M, double& out) {
-  const int odd = ~E & 1;  // s = M 2^(E - 1075); E - 1075 is odd when E is even
-  const uint64_t N = M << odd;  // s = N 2^p with p even, N in [2^52, 2^54)
-  const int p = E - 1075 - odd;
+// Reciprocal square root in fixed point: for s = M 2^(E - 1075) (M in [2^52, 2^53))
+// writes s = N 2^p with p even and N in [2^52, 2^54), and Y2 = 2^63 / sqrt(n),
+// n = N 2^-52, to a relative error below 2^-59; false when the seed check fails.
+GH_EMU_HD bool rsqrt_fixed(int E, uint64_t M, int& odd, uint64_t& N, int& p, uint64_t& Y2) {
+  odd = ~E & 1;  // s = M 2^(E - 1075); E - 1075 is odd when E is even
+  N = M << odd;
+  p = E - 1075 - odd;
 
   // seed: y0 ~ 1/sqrt(n), n = N 2^-52, as Y0 = y0 2^30
   const float nf = bitsf(0x3F800000u + ((uint32_t)odd << 23) + ((uint32_t)(M >> 29) & 0x7FFFFFu));
@@ -130,8 +130,18 @@ GH_EMU_HD bool inv_cube_core(int E, uint64_t M, double& out) {
   // Newton step 2: h2 = 1 - n y1^2 as H2 = h2 2^62 (|h2| < 2^-37, fits 32 bits)
   const uint64_t Y1sq = umulhi(Y1, Y1);  // y1^2 2^62 < 2^62
   const int32_t H2 = (int32_t)(uint32_t)((1ull << 62) - umulhi(N << 10, Y1sq << 2));
-  uint64_t Y2 = Y1 + (uint64_t)(((int64_t)(int32_t)(Y1 >> 32) * H2) >> 31);
+  Y2 = Y1 + (uint64_t)(((int64_t)(int32_t)(Y1 >> 32) * H2) >> 31);
   if (Y2 >= (1ull << 63)) Y2 = (1ull << 63) - 1;
+  return true;
+}
+
+// RN(RN(1/s) / RN(sqrt(s))) into `out` for s = M 2^(E - 1075) with M in
+// [2^52, 2^53) and 446 <= E <= 1624 (the caller checks the range); false when a
+// check fails (then `out` is untouched).
+GH_EMU_HD bool inv_cube_core(int E, uint64_t M, double& out) {
+  int odd, p;
+  uint64_t N, Y2;
+  if (!rsqrt_fixed(E, M, odd, N, p, Y2)) return false;
 
   // square root: sqrt(s) = B 2^(p/2 - 26), B = RN(sqrt(X) / 2), X = N 2^54, i.e.
   // c = 2B - 1 <= sqrt(X) < c + 2
@@ -196,6 +206,30 @@ GH_EMU_HD bool inv_cube_rn(double s, double& out) {
   const int E = (int)(bits >> 52);  // biased exponent; the sign bit makes it >= 2048
   if ((unsigned)(E - 446) > 1178u) return false;  // 2^-577 <= s < 2^602
   return inv_cube_core(E, (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull, out);
+}
+
+// s^(-3/2) within about half an ulp (not correctly rounded: the tree walk's FP64
+// interactions, which sum in their own order anyway); false outside [2^-577, 2^602).
+GH_EMU_HD bool rsqrt_cube(double s, double& out) {
+  const uint64_t bits = dbits(s);
+  const int E = (int)(bits >> 52);
+  if ((unsigned)(E - 446) > 1178u) return false;
+  int odd, p;
+  uint64_t N, Y2;
+  if (!rsqrt_fixed(E, (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull, odd, N, p, Y2)) return false;
+  // y^3 = Y3 2^-62, y = 1/sqrt(n) in (1/2, 1]
+  const uint64_t Y3 = umulhi(umulhi(Y2, Y2) << 1, Y2);
+#ifdef __CUDA_ARCH__
+  const int lz = __clzll((long long)Y3);
+#else
+  const int lz = __builtin_clzll(Y3);
+#endif
+  const uint64_t T = Y3 << lz;  // in [2^63, 2^64)
+  const uint64_t m = (T >> 11) + ((T >> 10) & 1);  // in [2^52, 2^53]
+  // s^(-3/2) = y^3 2^(-3 (26 + p/2)) = m 2^(11 - 62 - lz - 78 - 3p/2)
+  const int k = -129 - lz - 3 * (p / 2);
+  out = bitsd(((uint64_t)(k + 1074) << 52) + m);
+  return true;
 }
 
 // ---------------------------------------------------------------------------

@@ -642,7 +642,7 @@ __device__ __forceinline__ double rsqrt_f64(double s) {
 // MIXED: accepted cells interact in FP32: the hi/lo split offset of the cell's
 // centre (keeps ~2^-48 of |x|) plus the FP32 offset of its centre of mass; partial
 // sums folded into a two-sum (hi, lo) accumulator every 32 interactions.  Otherwise
-// FP64 with a Newton-refined rsqrt.
+// FP64 with s^(-3/2) from the integer-pipe reciprocal square root (f64emu.cuh).
 // The opening decisions are the same exact ones in both forms.
 constexpr int TW_FOLD = 32;
 
@@ -733,8 +733,12 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
           const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
           const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
           if (!GUARD || s != 0.0) {
-            const double y = rsqrt_f64(s);
-            const double f = M.w * (y * (y * y));
+            double y3;  // s^(-3/2) on the integer pipes, FP64 Newton steps outside its range
+            if (!emu::rsqrt_cube(s, y3)) {
+              const double y = rsqrt_f64(s);
+              y3 = y * (y * y);
+            }
+            const double f = M.w * y3;
             ax = fma(f, dx, ax);
             ay = fma(f, dy, ay);
             az = fma(f, dz, az);

@@ -70,7 +70,7 @@ int main(int argc, char** argv) {
   const double special[] = {0.0, -0.0, -1.0, INFINITY, NAN, 4.9406564584124654e-324, 2.2250738585072014e-308,
                             1.7976931348623157e308};
   for (double s : special) check(s);
-  const long long per = cases / 5;
+  const long long per = cases / 6;
   // uniform significand and exponent over the fast range and beyond
   for (long long i = 0; i < per; i++) {
     const uint64_t b = (next_u64() & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(300 + next_u64() % 1450) << 52);
@@ -162,6 +162,25 @@ int main(int argc, char** argv) {
     gh::emu::add_pos_rn(E, M, E1, M1, E2, M2);
     if ((((uint64_t)(E2 - 1) << 52) + M2) != bits_of(s3)) {
       if (n_wrong < 10) printf("WRONG sum3 %.17g %.17g %.17g\n", d[0], d[1], d[2]);
+      n_wrong++;
+    }
+  }
+  // s^(-3/2) for the tree walk: within 1 ulp of the correctly rounded value (long double)
+  for (long long i = 0; i < per; i++) {
+    const uint64_t b = (next_u64() & 0x000FFFFFFFFFFFFFull) | ((uint64_t)(446 + next_u64() % 1179) << 52);
+    double s;
+    memcpy(&s, &b, 8);
+    double got;
+    n_cases++;
+    if (!gh::emu::rsqrt_cube(s, got)) {
+      n_fallback++;
+      continue;
+    }
+    const long double ref = 1.0L / ((long double)s * sqrtl((long double)s));
+    const double want = (double)ref;
+    const long long ulps = (long long)bits_of(got) - (long long)bits_of(want);
+    if (ulps > 1 || ulps < -1) {
+      if (n_wrong < 10) printf("WRONG rsqrt_cube s=%.17g got=%.17g want=%.17g\n", s, got, want);
       n_wrong++;
     }
   }
