@@ -1,7 +1,7 @@
 // Correctly rounded FP64 reciprocal, square root and quotient on the integer
 // pipes, for the softened inverse cube of the FP64 direct sum:
 //
-//     inv = RN( RN(1/s) / RN(sqrt(s)) )      (gravhopper/_jbgrav.c:176-178, :338-342)
+//     inv = RN( RN(1/s) / RN(sqrt(s)) )      (gravhopper/_jbgrav.c:166, :330)
 //
 // GB300 issues FP64 at 1/64 of the FP32 rate, and the two IEEE divisions and the
 // square root take more than half of the FP64 instructions of a pair.  Here the
@@ -319,7 +319,7 @@ GH_EMU_HD bool unpack_eps2(double eps2, int& E, uint64_t& M) {
 }
 
 // inv = RN(RN(1/s) / RN(sqrt(s))) with s = RN(RN(RN(dx^2 + dy^2) + dz^2) + eps2),
-// the pair factor of gravhopper/_jbgrav.c:170-178.  eps2 is given unpacked
+// the pair factor of gravhopper/_jbgrav.c:159-166.  eps2 is given unpacked
 // (eps2_E = 0 for eps2 = 0; otherwise 2^-500 <= eps2 < 2^502).  False when a
 // component is zero or outside [2^-250, 2^251), or a check fails.
 GH_EMU_HD bool pair_inv_cube_rn(double dx, double dy, double dz, int eps2_E, uint64_t eps2_M, double& out) {

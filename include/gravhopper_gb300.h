@@ -199,7 +199,7 @@ int gh_measure_l2_read(double* bytes_per_s, void* stream);
 
 /* Self-check of the integer-pipe softened inverse cube RN(RN(1/s)/RN(sqrt(s))) used
  * by the FP64 direct sum (no counterpart in the reference, whose C code evaluates
- * 1.0/s/sqrt(s) with the FPU, gravhopper/_jbgrav.c:170-178): n seeded inputs on the
+ * 1.0/s/sqrt(s) with the FPU, gravhopper/_jbgrav.c:159-166): n seeded inputs on the
  * current device compared bit for bit with the native IEEE operations, half of them
  * also through the integer-pipe squared distance s = dx^2 + dy^2 + dz^2 + eps^2.
  * Writes the number of differing results and of in-range inputs that took the

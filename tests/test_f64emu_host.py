@@ -1,6 +1,6 @@
 """The integer-pipe FP64 inverse cube (gravhopper_gb300/csrc/f64emu.cuh) is pure
 integer arithmetic apart from its FP32 rsqrt seed, so its host build must reproduce
-the IEEE expression 1.0 / s / sqrt(s) of gravhopper/_jbgrav.c:176-178 bit for bit.
+the IEEE expression 1.0 / s / sqrt(s) of gravhopper/_jbgrav.c:166 bit for bit.
 The check program runs random, boundary and near-midpoint inputs; with the seed
 perturbed well beyond the FP32 approximation's error the range checks send inputs
 to the native path, and no confirmed result may differ."""
