@@ -268,7 +268,10 @@ static int launch_f64(const double* spos, const double* smass, int64_t np, const
   GH_TRY(device_info(&di));
   const int64_t want = 2LL * di.num_sms;  // CTAs for a full machine
   int form = g_f64_form;
-  if (form < 0) form = blocks < want ? 1 : 0;
+  // The thread-per-target kernel (90 registers, 5 CTAs per SM) fills the machine in
+  // whole waves only from about 8 CTAs per SM; below that the CTA-wide kernel is
+  // faster (N = 131,072: 447 against 562 ms; 262,144: 1780 against 1854 ms).
+  if (form < 0) form = blocks < 8LL * di.num_sms ? 1 : 0;
   prof_begin(st);
   if (form == 0) {
     direct_f64_kernel<SELF, Epi><<<(unsigned)blocks, F64_THREADS, 0, st>>>(spos, smass, np, tpos, nt,
