@@ -194,22 +194,26 @@ __global__ void __launch_bounds__(F64_THREADS)
     if (ti[r] < nt) epi(ti[r], ax[r], ay[r], az[r]);
 }
 
-// FP64 form for few targets (fewer than two CTAs of the kernel above per SM): the
-// pair terms (m_j d) inv are computed by all threads of the CTA into shared memory,
-// then summed in ascending j by one thread per (target, component), so the sums are
-// the reference's own.  A self pair contributes +0.0, which leaves every sum
-// unchanged: a round-to-nearest sum started at +0.0 is never -0.0.
+// FP64 form for few targets (fewer than eight CTAs of the kernel above per SM): the
+// pair terms (m_j d) inv of a chunk of sources are computed by warps 1-7 into shared
+// memory while warp 0 adds the previous chunk's terms in ascending j, one lane per
+// (target, component), so the sums are the reference's own.  Two term buffers, one
+// barrier per chunk.  A self pair contributes +0.0, which leaves every sum unchanged:
+// a round-to-nearest sum started at +0.0 is never -0.0.
 constexpr int F64O_THREADS = 256;
+constexpr int F64O_WORKERS = F64O_THREADS - 32;  // warps 1-7 compute pair terms
+constexpr int F64O_TERMS = 2 * F64O_WORKERS;     // pair terms per chunk: two per worker
 
 template <bool SELF, int TB, class Epi>
 __global__ void __launch_bounds__(F64O_THREADS)
     direct_f64_ordered_kernel(const double* __restrict__ spos, const double* __restrict__ smass, int64_t np,
                               const double* __restrict__ tpos, int64_t nt, double eps2, Epi epi) {
-  static_assert(3 * TB <= 32, "the summing threads form one warp");
-  constexpr int F64O_JC = 1024 / TB;      // sources per chunk: 1024 pair terms per chunk
-  constexpr int F64O_JP = F64O_JC + 1;    // padded rows: the summing threads hit distinct banks
-  __shared__ dvec4 src[F64O_JC];
-  __shared__ double term[3 * TB][F64O_JP];
+  static_assert(3 * TB <= 32, "the summing lanes form one warp");
+  static_assert(F64O_TERMS % TB == 0, "whole sources per chunk");
+  constexpr int JC = F64O_TERMS / TB;  // sources per chunk
+  constexpr int JP = JC + 1;           // padded rows: the summing lanes hit distinct banks
+  __shared__ dvec4 src[2][JC];
+  __shared__ double term[2][3 * TB][JP];
   __shared__ double tp[TB][3];
   __shared__ double res[3 * TB];
   const int tid = threadIdx.x;
@@ -218,48 +222,64 @@ __global__ void __launch_bounds__(F64O_THREADS)
     const int64_t ti = t0 + tid / 3;
     tp[tid / 3][tid % 3] = ti < nt ? tpos[3 * ti + tid % 3] : 0.0;
   }
-  double sum = 0.0;  // threads < 3 TB: target tid / 3, component tid % 3
+  const int w = tid - 32;  // worker index (warps 1-7)
+  if (w >= 0) {
+    for (int k = w; k < JC; k += F64O_WORKERS)
+      if (k < np) src[0][k] = make_dvec4(spos[3 * k], spos[3 * k + 1], spos[3 * k + 2], smass[k]);
+  }
+  __syncthreads();
+  double sum = 0.0;  // lanes < 3 TB of warp 0: target tid / 3, component tid % 3
   int e2E;
   uint64_t e2M;
   const bool emu_ok = emu::unpack_eps2(eps2, e2E, e2M);  // integer-pipe pair factor usable
-  for (int64_t j0 = 0; j0 < np; j0 += F64O_JC) {
-    __syncthreads();
-    for (int k = tid; k < F64O_JC; k += F64O_THREADS) {
-      const int64_t j = j0 + k;
-      if (j < np) src[k] = make_dvec4(spos[3 * j], spos[3 * j + 1], spos[3 * j + 2], smass[j]);
-    }
-    __syncthreads();
-    const int jn = (np - j0) < F64O_JC ? (int)(np - j0) : F64O_JC;
-    for (int q = tid; q < TB * F64O_JC; q += F64O_THREADS) {
-      const int t = q / F64O_JC, k = q % F64O_JC;
-      if (k >= jn) continue;
-      double vx = 0.0, vy = 0.0, vz = 0.0;
-      if (!(SELF && j0 + k == t0 + t)) {
-        const dvec4 s = src[k];
-        const double dx = dsub(s.x, tp[t][0]);
-        const double dy = dsub(s.y, tp[t][1]);
-        const double dz = dsub(s.z, tp[t][2]);
-        double inv;
-        if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
-          double r2 = dmul(dx, dx);
-          r2 = dadd(r2, dmul(dy, dy));
-          r2 = dadd(r2, dmul(dz, dz));
-          const double ss = dadd(r2, eps2);
-          if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+  const int64_t nchunks = (np + JC - 1) / JC;
+  for (int64_t c = 0; c <= nchunks; c++) {
+    if (w >= 0) {
+      if (c + 1 < nchunks) {  // next chunk's sources into the other buffer
+        const int64_t j1 = (c + 1) * JC;
+        for (int k = w; k < JC; k += F64O_WORKERS) {
+          const int64_t j = j1 + k;
+          if (j < np) src[(c + 1) & 1][k] = make_dvec4(spos[3 * j], spos[3 * j + 1], spos[3 * j + 2], smass[j]);
         }
-        vx = dmul(dmul(s.w, dx), inv);
-        vy = dmul(dmul(s.w, dy), inv);
-        vz = dmul(dmul(s.w, dz), inv);
       }
-      term[3 * t + 0][k] = vx;
-      term[3 * t + 1][k] = vy;
-      term[3 * t + 2][k] = vz;
-    }
-    __syncthreads();
-    if (tid < 3 * TB) {
-      const double* row = term[tid];
+      if (c < nchunks) {
+        const int64_t j0 = c * JC;
+        const int jn = (np - j0) < JC ? (int)(np - j0) : JC;
+        const dvec4* sc = src[c & 1];
+        double(*tc)[JP] = term[c & 1];
+        for (int q = w; q < TB * JC; q += F64O_WORKERS) {
+          const int t = q / JC, k = q % JC;
+          if (k >= jn) continue;
+          double vx = 0.0, vy = 0.0, vz = 0.0;
+          if (!(SELF && j0 + k == t0 + t)) {
+            const dvec4 s = sc[k];
+            const double dx = dsub(s.x, tp[t][0]);
+            const double dy = dsub(s.y, tp[t][1]);
+            const double dz = dsub(s.z, tp[t][2]);
+            double inv;
+            if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
+              double r2 = dmul(dx, dx);
+              r2 = dadd(r2, dmul(dy, dy));
+              r2 = dadd(r2, dmul(dz, dz));
+              const double ss = dadd(r2, eps2);
+              if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+            }
+            vx = dmul(dmul(s.w, dx), inv);
+            vy = dmul(dmul(s.w, dy), inv);
+            vz = dmul(dmul(s.w, dz), inv);
+          }
+          tc[3 * t + 0][k] = vx;
+          tc[3 * t + 1][k] = vy;
+          tc[3 * t + 2][k] = vz;
+        }
+      }
+    } else if (c >= 1 && tid < 3 * TB) {  // previous chunk's terms, in order
+      const int64_t j0 = (c - 1) * JC;
+      const int jn = (np - j0) < JC ? (int)(np - j0) : JC;
+      const double* row = term[(c - 1) & 1][tid];
       for (int k = 0; k < jn; k++) sum = dadd(sum, row[k]);
     }
+    __syncthreads();
   }
   if (tid < 3 * TB) res[tid] = sum;
   __syncthreads();
