@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Direct-sum Gpair/s & tree particle-steps/s, mixed vs FP64, 1 GB300 @ <=1e-6 err"
 UNIT = "Gpair/s"
 PAIR_OPS = 12  # FP32 FMA-pipe lane-ops per pair: 3 sub, 3 fma, 3 mul, 3 fma
+PAIR_OPS_FP64 = 12  # FP64-pipe ops per pair of the FP64 form: 3 sub, 6 mul, 3 add
 
 
 def parse():
@@ -250,16 +251,23 @@ def main():
 
     kern_avg_s = kern_ms / max(kern_n, 1) * 1e-3
     achieved = pairs / kern_avg_s / 1e9
-    peak = fp32_peak / PAIR_OPS / 1e9
+    mixed = args.precision == "mixed"
+    # mixed: 12 FP32 FMA-pipe lane-ops per pair; FP64: the 12 of the reference's pair
+    # operations that stay on the FP64 pipe (squared distance, division and square
+    # root run as exact integer arithmetic)
+    peak = (fp32_peak if mixed else fp64_peak) / (PAIR_OPS if mixed else PAIR_OPS_FP64) / 1e9
     # DRAM bytes (read + write) of one launch of the fused DKD kernel at N = 1,048,576,
     # from one single-pass ncu capture (dram__bytes_read.sum 78.47 MB + write 29.32 MB;
     # profiles/direct_mixed_bench_n1048576_launches.md); other sizes: not captured
     traffic = 107.79e6 if (args.precision == "mixed" and n == 1 << 20) else None
-    roofline = {"bound": "fp32", "kernel": "direct_mixed_kernel" if args.precision == "mixed" else
-                "direct_f64_kernel", "achieved": achieved, "peak": peak, "unit": UNIT,
+    roofline = {"bound": "fp32" if mixed else "fp64",
+                "kernel": "direct_mixed_kernel" if mixed else "direct_f64_kernel",
+                "achieved": achieved, "peak": peak, "unit": UNIT,
                 "frac": achieved / peak, "traffic": traffic,
-                "peak_source": f"measured live: f32x2 FMA chains, {fp32_peak / 1e12:.1f} T lane-op/s "
-                               f"/ {PAIR_OPS} lane-ops per pair",
+                "peak_source": (f"measured live: f32x2 FMA chains, {fp32_peak / 1e12:.1f} T lane-op/s "
+                                f"/ {PAIR_OPS} lane-ops per pair") if mixed else
+                               (f"measured live: FP64 FMA chains, {fp64_peak / 1e12:.2f} T lane-op/s "
+                                f"/ {PAIR_OPS_FP64} FP64-pipe ops per pair"),
                 "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
 
     secondary = {}
@@ -302,6 +310,7 @@ def measure_secondary(ic, dev, fp64_peak, mixed_gpair):
     out["fp64_n"] = 65536
     out["fp64_gpair_s"] = g64
     out["fp64_lane_ops_peak_t"] = fp64_peak / 1e12
+    out["fp64_pipe_frac"] = g64 * 1e9 * PAIR_OPS_FP64 / fp64_peak  # 12 FP64-pipe ops per pair
     if mixed_gpair:
         out["mixed_over_fp64"] = mixed_gpair / g64
     # Mixed-form error against the FP64 form (bit-identical to the oracle) on 4096

@@ -153,6 +153,29 @@ def test_fp64_forms_bit_exact(lib, cuda, form):
         _capi.call("gh_direct_set_fp64_form", -1)
 
 
+@pytest.mark.parametrize("form", [0, 1])
+def test_fp64_zero_components_bit_exact(lib, cuda, form):
+    """Exact-zero coordinate differences (a planar disk, a lattice) send those pairs to
+    the native IEEE operations inside the FP64 kernels; mixed with integer-pipe pairs
+    the sums are still the reference's bits."""
+    from gravhopper_gb300 import _capi, _jbgrav
+    rng = np.random.default_rng(8)
+    planar = np.column_stack([rng.normal(size=(600, 2)), np.zeros(600)])
+    g = np.arange(6, dtype=np.float64) * 0.25
+    lattice = np.array(np.meshgrid(g, g, g, indexing="ij")).reshape(3, -1).T.copy()
+    _capi.call("gh_direct_set_fp64_form", form)
+    try:
+        for pos in (planar, lattice):
+            m = rng.uniform(0.5, 2.0, size=len(pos))
+            for eps in (0.0, 5e-2):
+                np.testing.assert_array_equal(_jbgrav.direct_summation(pos, m, eps),
+                                              oracle.direct_summation(pos, m, eps))
+            np.testing.assert_array_equal(_jbgrav.direct_summation_position(pos, m, pos[:50], 0.0),
+                                          oracle.direct_summation_position(pos, m, pos[:50], 0.0))
+    finally:
+        _capi.call("gh_direct_set_fp64_form", -1)
+
+
 def test_every_mixed_shape(lib, cuda):
     """Every compiled tile shape of the mixed kernel (packed and scalar loops) meets the
     mixed tolerance, for self forces and target points."""
