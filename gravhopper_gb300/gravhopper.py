@@ -27,6 +27,10 @@ from . import ics as _ics
 from . import jbgrav
 from . import units as U
 
+# Snapshot history per device run segment (positions and velocities, 48 bytes per
+# particle and step); one segment's copy to the host overlaps the next one's steps.
+HISTORY_SEGMENT_BYTES = 256 << 20
+
 
 class GravHopperException(Exception):
     """Parent class for all error exceptions."""
@@ -194,17 +198,49 @@ class Simulation(object):
         x = torch.from_numpy(np.ascontiguousarray(self._pos[t0])).to(dev)
         v = torch.from_numpy(np.ascontiguousarray(self._vel[t0])).to(dev)
         m = torch.from_numpy(np.ascontiguousarray(self._mass)).to(dev)
-        hist = engine.run_dkd(x, v, m, N, self._dt(), self._eps(), algorithm=self.params["algorithm"],
-                              precision=self.params["precision"], theta=self.params["theta"],
-                              hist_stride=1)
-        hp, hv = hist
-        # copy straight into the history arrays (one device -> host copy each)
-        torch.from_numpy(self._pos[t0 + 1:t0 + N + 1]).copy_(hp)
-        torch.from_numpy(self._vel[t0 + 1:t0 + N + 1]).copy_(hv)
+        # Segments of about 256 MB of snapshot history: segment k is copied into the
+        # history arrays by a helper thread on a side stream while segment k + 1 runs
+        # (the copies into pageable host memory return only when complete).
+        seg = max(1, min(N, HISTORY_SEGMENT_BYTES // max(1, 48 * self.Np)))
+        pending, pool, copy_stream = None, None, None
+        done = 0
+        try:
+            while done < N:
+                k = min(seg, N - done)
+                hp, hv = engine.run_dkd(x, v, m, k, self._dt(), self._eps(), algorithm=self.params["algorithm"],
+                                        precision=self.params["precision"], theta=self.params["theta"],
+                                        hist_stride=1)
+                if k == N:  # one segment: copy straight into the history arrays
+                    torch.from_numpy(self._pos[t0 + 1:t0 + N + 1]).copy_(hp)
+                    torch.from_numpy(self._vel[t0 + 1:t0 + N + 1]).copy_(hv)
+                    break
+                if pool is None:
+                    from concurrent.futures import ThreadPoolExecutor
+                    pool = ThreadPoolExecutor(max_workers=1)
+                    copy_stream = torch.cuda.Stream(device=dev)
+                ready = torch.cuda.Event()
+                ready.record()
+                if pending is not None:
+                    pending.result()
+                pending = pool.submit(self._copy_history, hp, hv, ready, copy_stream, t0 + done + 1)
+                done += k
+            if pending is not None:
+                pending.result()
+        finally:
+            if pool is not None:
+                pool.shutdown(wait=True)
         dt = self._dt()
         for k in range(t0 + 1, t0 + N + 1):
             self._times[k] = self._times[k - 1] + dt
         self.timestep = t0 + N
+
+    def _copy_history(self, hp, hv, ready, stream, first):
+        import torch
+        with torch.cuda.stream(stream):
+            stream.wait_event(ready)
+            k = hp.shape[0]
+            torch.from_numpy(self._pos[first:first + k]).copy_(hp)
+            torch.from_numpy(self._vel[first:first + k]).copy_(hv)
 
     def init_run(self, Nsnap=None):
         """Initialise an N-body run (gravhopper.py:324-342)."""

@@ -112,6 +112,30 @@ def test_simulation_with_external_force_matches_restatement(golden, lib, cuda):
     np.testing.assert_array_equal(sim.velocities[6], v)
 
 
+def test_segmented_history_copy(golden, lib, cuda, monkeypatch):
+    """Simulation.run in history segments (copies overlapped with the next segment's
+    steps) gives every snapshot of the one-segment run, and the reference's bits."""
+    import gravhopper_gb300 as gh
+    from gravhopper_gb300 import gravhopper as ghmod
+    n = 300
+    ic = {"pos": golden["plummer_pos"][:n], "vel": golden["plummer_vel"][:n], "mass": golden["plummer_mass"][:n]}
+
+    def run(seg_bytes):
+        monkeypatch.setattr(ghmod, "HISTORY_SEGMENT_BYTES", seg_bytes)
+        sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct", precision="fp64")
+        sim.add_IC(ic)
+        sim.run(30)
+        return sim
+
+    whole, parts = run(256 << 20), run(48 * n * 7)  # one segment; segments of 7 steps
+    np.testing.assert_array_equal(parts.positions, whole.positions)
+    np.testing.assert_array_equal(parts.velocities, whole.velocities)
+    for k in (7, 8, 30):
+        rx, rv = oracle.dkd_run(ic["pos"], ic["vel"], ic["mass"], 0.005, 5e-5, k)
+        np.testing.assert_array_equal(parts.positions[k], rx)
+        np.testing.assert_array_equal(parts.velocities[k], rv)
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_momentum_diagnostics_conserved(lib, cuda, precision):
     """Pairwise central forces conserve linear and angular momentum; the leapfrog keeps
