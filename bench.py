@@ -380,7 +380,9 @@ def measure_tree(dev, n=1 << 20, steps=2):
         for prec in ("mixed", "fp64"):
             x = torch.from_numpy(ic["pos"]).to(dev)
             v = torch.from_numpy(ic["vel"]).to(dev)
-            engine.run_dkd(x, v, m, 1, 0.5, 0.1, algorithm="tree", theta=theta, precision=prec)
+            # warm-up with the timed call's own step count (every kernel variant loaded)
+            engine.run_dkd(x, v, m, steps, 0.5, 0.1, algorithm="tree", theta=theta, precision=prec)
+            torch.cuda.synchronize()
             _capi.kernel_timing_collect()
             _capi.kernel_timing(True)
             t = _timed(lambda: engine.run_dkd(x, v, m, steps, 0.5, 0.1, algorithm="tree", theta=theta,
