@@ -139,6 +139,31 @@ constexpr int F64_THREADS = 128;
 constexpr int F64_R = 2;
 constexpr int F64_JT = 128;
 
+// The pair terms RN(RN(m d_k) inv) of one (target, source) pair with the reference's
+// operations (gravhopper/_jbgrav.c:159-166, 181): d = x_j - x_i, then s and
+// inv = 1/s/sqrt(s) on the integer pipes (f64emu.cuh) with the native IEEE operations
+// for the inputs that path leaves out.  Without the self-pair exclusion (target
+// points) s = 0 gives zero terms (:325-331).
+template <bool SELF>
+__device__ __forceinline__ void f64_pair_terms(const dvec4& s, double tx, double ty, double tz, double eps2,
+                                               bool emu_ok, int e2E, uint64_t e2M, double& vx, double& vy,
+                                               double& vz) {
+  const double dx = dsub(s.x, tx);
+  const double dy = dsub(s.y, ty);
+  const double dz = dsub(s.z, tz);
+  double inv;
+  if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
+    double r2 = dmul(dx, dx);
+    r2 = dadd(r2, dmul(dy, dy));
+    r2 = dadd(r2, dmul(dz, dz));
+    const double ss = dadd(r2, eps2);
+    if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
+  }
+  vx = dmul(dmul(s.w, dx), inv);
+  vy = dmul(dmul(s.w, dy), inv);
+  vz = dmul(dmul(s.w, dz), inv);
+}
+
 template <bool SELF, class Epi>
 __global__ void __launch_bounds__(F64_THREADS)
     direct_f64_kernel(const double* __restrict__ spos, const double* __restrict__ smass, int64_t np,
@@ -172,20 +197,11 @@ __global__ void __launch_bounds__(F64_THREADS)
 #pragma unroll
       for (int r = 0; r < F64_R; r++) {
         if (SELF && (j0 + k) == ti[r]) continue;
-        double dx = dsub(s.x, tx[r]);
-        double dy = dsub(s.y, ty[r]);
-        double dz = dsub(s.z, tz[r]);
-        double inv;
-        if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
-          double r2 = dmul(dx, dx);
-          r2 = dadd(r2, dmul(dy, dy));
-          r2 = dadd(r2, dmul(dz, dz));
-          const double ss = dadd(r2, eps2);
-          if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
-        }
-        ax[r] = dadd(ax[r], dmul(dmul(s.w, dx), inv));
-        ay[r] = dadd(ay[r], dmul(dmul(s.w, dy), inv));
-        az[r] = dadd(az[r], dmul(dmul(s.w, dz), inv));
+        double vx, vy, vz;
+        f64_pair_terms<SELF>(s, tx[r], ty[r], tz[r], eps2, emu_ok, e2E, e2M, vx, vy, vz);
+        ax[r] = dadd(ax[r], vx);
+        ay[r] = dadd(ay[r], vy);
+        az[r] = dadd(az[r], vz);
       }
     }
   }
@@ -251,23 +267,8 @@ __global__ void __launch_bounds__(F64O_THREADS)
           const int t = q / JC, k = q % JC;
           if (k >= jn) continue;
           double vx = 0.0, vy = 0.0, vz = 0.0;
-          if (!(SELF && j0 + k == t0 + t)) {
-            const dvec4 s = sc[k];
-            const double dx = dsub(s.x, tp[t][0]);
-            const double dy = dsub(s.y, tp[t][1]);
-            const double dz = dsub(s.z, tp[t][2]);
-            double inv;
-            if (!(emu_ok && emu::pair_inv_cube_rn(dx, dy, dz, e2E, e2M, inv))) {
-              double r2 = dmul(dx, dx);
-              r2 = dadd(r2, dmul(dy, dy));
-              r2 = dadd(r2, dmul(dz, dz));
-              const double ss = dadd(r2, eps2);
-              if (!emu::inv_cube_rn(ss, inv)) inv = (!SELF && ss == 0.0) ? 0.0 : ddiv(ddiv(1.0, ss), dsqrt(ss));
-            }
-            vx = dmul(dmul(s.w, dx), inv);
-            vy = dmul(dmul(s.w, dy), inv);
-            vz = dmul(dmul(s.w, dz), inv);
-          }
+          if (!(SELF && j0 + k == t0 + t))
+            f64_pair_terms<SELF>(sc[k], tp[t][0], tp[t][1], tp[t][2], eps2, emu_ok, e2E, e2M, vx, vy, vz);
           tc[3 * t + 0][k] = vx;
           tc[3 * t + 1][k] = vy;
           tc[3 * t + 2][k] = vz;
