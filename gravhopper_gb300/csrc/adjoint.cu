@@ -63,9 +63,12 @@ __global__ void __launch_bounds__(AJ_THREADS)
       const dvec4 P = sp[t], L = sl[t];
       const double dx = P.x - xk, dy = P.y - yk, dz = P.z - zk;
       const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
-      const double r = rsqrt_nr(s);
-      const double r2 = r * r;
-      const double q = r2 * r;
+      double r2, q;  // s^-1 and s^(-3/2) on the integer pipes; FP64 Newton steps outside its range
+      if (!emu::rsqrt_powers(s, r2, q)) {
+        const double r = rsqrt_nr(s);
+        r2 = r * r;
+        q = r2 * r;
+      }
       const double p = 3.0 * q * r2;
       const double ux = mk * L.x - P.w * lxk, uy = mk * L.y - P.w * lyk, uz = mk * L.z - P.w * lzk;
       const double du = fma(dx, ux, fma(dy, uy, dz * uz));

@@ -232,6 +232,30 @@ GH_EMU_HD bool rsqrt_cube(double s, double& out) {
   return true;
 }
 
+// s^(-1) and s^(-3/2), each within about half an ulp (the FP64 adjoint's pair factors);
+// false outside [2^-577, 2^602).
+GH_EMU_HD bool rsqrt_powers(double s, double& inv1, double& inv3) {
+  const uint64_t bits = dbits(s);
+  const int E = (int)(bits >> 52);
+  if ((unsigned)(E - 446) > 1178u) return false;
+  int odd, p;
+  uint64_t N, Y2;
+  if (!rsqrt_fixed(E, (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull, odd, N, p, Y2)) return false;
+  const uint64_t Y2sq = umulhi(Y2, Y2);         // y^2 2^62, y = 1/sqrt(n) in (1/2, 1]
+  const uint64_t Y3 = umulhi(Y2sq << 1, Y2);    // y^3 2^62
+#ifdef __CUDA_ARCH__
+  const int l2 = __clzll((long long)Y2sq), l3 = __clzll((long long)Y3);
+#else
+  const int l2 = __builtin_clzll(Y2sq), l3 = __builtin_clzll(Y3);
+#endif
+  const uint64_t T2 = Y2sq << l2, T3 = Y3 << l3;  // in [2^63, 2^64)
+  const uint64_t m2 = (T2 >> 11) + ((T2 >> 10) & 1), m3 = (T3 >> 11) + ((T3 >> 10) & 1);
+  // s^-1 = y^2 2^(-52 - p) = m2 2^(11 - 62 - l2 - 52 - p); s^(-3/2) as in rsqrt_cube
+  inv1 = bitsd(((uint64_t)(-103 - l2 - p + 1074) << 52) + m2);
+  inv3 = bitsd(((uint64_t)(-129 - l3 - 3 * (p / 2) + 1074) << 52) + m3);
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // The softened squared distance s = RN(RN(RN(dx^2 + dy^2) + dz^2) + eps^2) with
 // every product and sum rounded as the FPU does (round to nearest even).  All terms

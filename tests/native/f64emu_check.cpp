@@ -183,6 +183,17 @@ int main(int argc, char** argv) {
       if (n_wrong < 10) printf("WRONG rsqrt_cube s=%.17g got=%.17g want=%.17g\n", s, got, want);
       n_wrong++;
     }
+    double p1, p3;  // s^-1 and s^(-3/2) together
+    if (!gh::emu::rsqrt_powers(s, p1, p3)) {
+      n_fallback++;
+      continue;
+    }
+    const long long u1 = (long long)bits_of(p1) - (long long)bits_of((double)(1.0L / (long double)s));
+    const long long u3 = (long long)bits_of(p3) - (long long)bits_of(want);
+    if (u1 > 1 || u1 < -1 || u3 > 1 || u3 < -1) {
+      if (n_wrong < 10) printf("WRONG rsqrt_powers s=%.17g\n", s);
+      n_wrong++;
+    }
   }
   printf("%lld %lld %lld %lld\n", n_cases, n_wrong, n_fallback, n_out);
   return n_wrong || n_out ? 1 : 0;
