@@ -298,7 +298,11 @@ __global__ void __launch_bounds__(AJ_THREADS)
       const dvec4 P = sp[t];
       const double dx = P.x - xk, dy = P.y - yk, dz = P.z - zk;
       const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
-      if (s > 0.0) phi = fma(-P.w, rsqrt_nr(s), phi);
+      if (s > 0.0) {
+        double y;  // s^(-1/2) on the integer pipes; FP64 Newton steps outside its range
+        if (!emu::rsqrt1(s, y)) y = rsqrt_nr(s);
+        phi = fma(-P.w, y, phi);
+      }
     }
   }
   if (valid) part[split * n + k] = phi;

@@ -232,6 +232,27 @@ GH_EMU_HD bool rsqrt_cube(double s, double& out) {
   return true;
 }
 
+// s^(-1/2) within about half an ulp (the FP64 potential); false outside
+// [2^-577, 2^602).
+GH_EMU_HD bool rsqrt1(double s, double& out) {
+  const uint64_t bits = dbits(s);
+  const int E = (int)(bits >> 52);
+  if ((unsigned)(E - 446) > 1178u) return false;
+  int odd, p;
+  uint64_t N, Y2;
+  if (!rsqrt_fixed(E, (bits & 0x000FFFFFFFFFFFFFull) | 0x0010000000000000ull, odd, N, p, Y2)) return false;
+#ifdef __CUDA_ARCH__
+  const int lz = __clzll((long long)Y2);
+#else
+  const int lz = __builtin_clzll(Y2);
+#endif
+  const uint64_t T = Y2 << lz;  // y 2^63 << lz, in [2^63, 2^64)
+  const uint64_t m = (T >> 11) + ((T >> 10) & 1);
+  // s^(-1/2) = y 2^(-26 - p/2) = m 2^(11 - 63 - lz - 26 - p/2)
+  out = bitsd(((uint64_t)(-78 - lz - p / 2 + 1074) << 52) + m);
+  return true;
+}
+
 // s^(-1) and s^(-3/2), each within about half an ulp (the FP64 adjoint's pair factors);
 // false outside [2^-577, 2^602).
 GH_EMU_HD bool rsqrt_powers(double s, double& inv1, double& inv3) {

@@ -183,6 +183,16 @@ int main(int argc, char** argv) {
       if (n_wrong < 10) printf("WRONG rsqrt_cube s=%.17g got=%.17g want=%.17g\n", s, got, want);
       n_wrong++;
     }
+    double r1;  // s^(-1/2)
+    if (!gh::emu::rsqrt1(s, r1)) {
+      n_fallback++;
+      continue;
+    }
+    const long long u0 = (long long)bits_of(r1) - (long long)bits_of((double)(1.0L / sqrtl((long double)s)));
+    if (u0 > 1 || u0 < -1) {
+      if (n_wrong < 10) printf("WRONG rsqrt1 s=%.17g\n", s);
+      n_wrong++;
+    }
     double p1, p3;  // s^-1 and s^(-3/2) together
     if (!gh::emu::rsqrt_powers(s, p1, p3)) {
       n_fallback++;
