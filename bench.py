@@ -13,8 +13,13 @@ Also reported on the same line:
   (``gh_direct_host``: pinned host -> device copy, force, device -> host copy),
 * ``roofline``: the mixed kernel against the FP32 FMA-pipe peak measured live
   (12 FMA-pipe lane-ops per pair),
-* ``secondary``: the FP64 form's Gpair/s (N = 65,536), the mixed form's error against
-  the FP64 form on sampled targets, the mixed/FP64 throughput ratio,
+* ``secondary``: the mixed form's error against the FP64 form on sampled targets,
+  energy drift, the tree, ensemble and adjoint measurements in detail,
+* ``tree``: particle-steps/s of tree DKD steps (Hernquist + disk, N = 1,048,576,
+  theta 0.7 and 0.5, mixed and FP64 walks) beside the reference tree on the host cores,
+* ``fp64``: the precision-matched number, the FP64 form (the reference's operation
+  order, bit-identical results) in Gpair/s at N = 262,144, with its FP64-pipe
+  fraction and its ratio to ``cpu_baseline``,
 * ``cpu_baseline``: the CPU oracle (a restatement of the reference's C loops) on the
   host cores, on a bounded sample of targets.
 
@@ -270,49 +275,93 @@ def main():
                                 f"/ {PAIR_OPS_FP64} FP64-pipe ops per pair"),
                 "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
 
-    secondary = {}
+    secondary, fp64 = {}, None
     if not args.no_secondary and rank == 0:
-        secondary = measure_secondary(ic, dev, fp64_peak, achieved if args.precision == "mixed" else None)
+        secondary = measure_secondary(ic, dev)
+        fp64 = measure_fp64(dev, fp64_peak)
 
     if rank == 0:
+        # long detail first, the headline extras last (a reader of the line's tail sees them)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": step_ms_max / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None,
                 "dtype": "f32" if args.precision == "mixed" else "f64",
                 "data": "synthetic", "config": _config(args), "roofline": roofline,
                 "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
-                "secondary": secondary}
-        line["cpu_baseline"] = cpu_baseline(n, args.cpu_targets)
+                "secondary": _rounded(secondary)}
+        if secondary.get("tree"):
+            line["tree"] = tree_summary(secondary["tree"])
+        cpu = cpu_baseline(n, args.cpu_targets)
+        if fp64:
+            fp64["vs_cpu_baseline"] = fp64["value"] / cpu["value"]
+            if args.precision == "mixed":
+                fp64["mixed_over_fp64"] = achieved / fp64["value"]
+            line["fp64"] = _rounded(fp64)
+        line["cpu_baseline"] = cpu
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def measure_secondary(ic, dev, fp64_peak, mixed_gpair):
-    """FP64-form throughput and mixed-form accuracy on this GPU."""
-    import numpy as np
+def _rounded(obj, digits=4):
+    """The same structure with floats rounded to `digits` significant digits."""
+    if isinstance(obj, float):
+        return float(f"{obj:.{digits}g}")
+    if isinstance(obj, dict):
+        return {k: _rounded(v, digits) for k, v in obj.items()}
+    if isinstance(obj, (list, tuple)):
+        return [_rounded(v, digits) for v in obj]
+    return obj
+
+
+def measure_fp64(dev, fp64_peak, n=262144, reps=2):
+    """The FP64 form (the reference's per-pair operation order, bit-identical results):
+    Gpair/s of the self-force of the N = 262,144 Plummer sphere, kernel-timed over
+    `reps` calls after one warm-up, and its fraction of the FP64 pipe measured live
+    (12 of the reference's pair operations stay on that pipe)."""
     import torch
 
     from gravhopper_gb300 import _capi, engine, ics
-    out = {}
-    # FP64 form throughput at N = 65,536 (one force evaluation, kernel-timed).
-    s = ics.plummer(65536, seed=7)
+    s = ics.plummer(n, seed=7)
     xs = torch.from_numpy(s["pos"]).to(dev)
     ms_ = torch.from_numpy(s["mass"]).to(dev)
     engine.direct_force(xs, ms_, 5e-5, precision="fp64")
     torch.cuda.synchronize()
     _capi.kernel_timing_collect()
     _capi.kernel_timing(True)
-    engine.direct_force(xs, ms_, 5e-5, precision="fp64")
+    for _ in range(reps):
+        engine.direct_force(xs, ms_, 5e-5, precision="fp64")
     _capi.kernel_timing(False)
-    kms, _ = _capi.kernel_timing_collect()
-    g64 = 65536.0 * 65535 / (kms * 1e-3) / 1e9
-    out["fp64_n"] = 65536
-    out["fp64_gpair_s"] = g64
-    out["fp64_lane_ops_peak_t"] = fp64_peak / 1e12
-    out["fp64_pipe_frac"] = g64 * 1e9 * PAIR_OPS_FP64 / fp64_peak  # 12 FP64-pipe ops per pair
-    if mixed_gpair:
-        out["mixed_over_fp64"] = mixed_gpair / g64
+    kms, kn = _capi.kernel_timing_collect()
+    sec = kms / max(kn, 1) * 1e-3
+    g64 = float(n) * (n - 1) / sec / 1e9
+    return {"workload": f"FP64 direct-sum self-force, Plummer sphere N={n} (bit-identical to the reference)",
+            "value": g64, "unit": UNIT, "ms_per_force": sec * 1e3, "forces_timed": kn,
+            "fp64_pipe_frac": g64 * 1e9 * PAIR_OPS_FP64 / fp64_peak,
+            "peak_source": f"measured live: FP64 FMA chains, {fp64_peak / 1e12:.3f} T lane-op/s / "
+                           f"{PAIR_OPS_FP64} FP64-pipe ops per pair"}
+
+
+def tree_summary(tree):
+    """Particle-steps/s of the tree steps, with the reference tree on the host cores."""
+    out = {"workload": f"tree DKD steps, Hernquist+disk N={tree['n']}", "unit": "particle-steps/s"}
+    for key in ("theta_0.7", "theta_0.5"):
+        t = tree.get(key, {})
+        row = {p: float(f"{t[p]['particle_steps_per_s']:.4g}") for p in ("mixed", "fp64") if p in t}
+        if "cpu_reference_s_per_step" in t:
+            row["cpu_reference"] = float(f"{tree['n'] / t['cpu_reference_s_per_step']:.4g}")
+            row["cpu_cores"] = t["cpu_reference_cores"]
+        out[key] = row
+    return out
+
+
+def measure_secondary(ic, dev):
+    """Mixed-form accuracy, energy drift, tree, ensemble and adjoint on this GPU."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import engine
+    out = {}
     # Mixed-form error against the FP64 form (bit-identical to the oracle) on 4096
     # sampled targets of the N = 1,048,576 system.
     n = ic["pos"].shape[0]

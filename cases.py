@@ -1,11 +1,11 @@
 """Run one engine workload a few times and print its timing (for profiling).
 
-    python -m gravhopper_gb300.cases direct   --n 131072 --reps 2   # mixed direct force
-    python -m gravhopper_gb300.cases direct64 --n 65536  --reps 1   # FP64 direct force
-    python -m gravhopper_gb300.cases dkd      --n 1048576 --reps 1  # mixed DKD step
-    python -m gravhopper_gb300.cases tree     --n 65536  --theta 0.7 --precision fp64
-    python -m gravhopper_gb300.cases ensemble --systems 64
-    python -m gravhopper_gb300.cases vjp      --n 16384
+    python cases.py direct   --n 131072 --reps 2   # mixed direct force
+    python cases.py direct64 --n 65536  --reps 1   # FP64 direct force
+    python cases.py dkd      --n 1048576 --reps 1  # mixed DKD step
+    python cases.py tree     --n 65536  --theta 0.7 --precision fp64
+    python cases.py ensemble --systems 64
+    python cases.py vjp      --n 16384
 
 Each case builds seeded inputs (Plummer spheres; Hernquist plus disk for the tree),
 runs one warm-up call and ``--reps`` timed calls on cuda:0, and prints one line of
@@ -14,7 +14,11 @@ milliseconds per call.
 from __future__ import annotations
 
 import argparse
+import os
+import sys
 import time
+
+sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
 
 
 def main(argv=None):
@@ -32,7 +36,7 @@ def main(argv=None):
 
     import torch
 
-    from . import _capi, engine, ics
+    from gravhopper_gb300 import _capi, engine, ics
     dev = torch.device("cuda", 0)
     _capi.load()
     _capi.call("gh_direct_set_fp64_form", a.fp64_form)
@@ -42,7 +46,7 @@ def main(argv=None):
     elif a.case == "tree":
         ic = ics.hernquist_disk(a.n, seed=1)
     if a.case == "ensemble":
-        from .ensemble import Ensemble
+        from gravhopper_gb300.ensemble import Ensemble
         e = Ensemble(ics.plummer_ensemble(a.systems, seed=0), device=dev)
         call = lambda: e.run(1, use_graph=False)  # noqa: E731
     else:

@@ -27,6 +27,9 @@ GH_PREC_MIXED = 1
 GH_ALGO_DIRECT = 0
 GH_ALGO_TREE = 1
 
+GH_INJECT_ALLOC = 1
+GH_INJECT_TREE_WAIT = 2
+
 PRECISIONS = {"fp64": GH_PREC_FP64, "mixed": GH_PREC_MIXED}
 ALGORITHMS = {"direct": GH_ALGO_DIRECT, "tree": GH_ALGO_TREE}
 
@@ -89,6 +92,8 @@ SIGNATURES = {
     "gh_check_inv_cube": (_int, [_i64, _u64, _vp, _vp]),
     "gh_tree_stats": (_int, [_int]),
     "gh_tree_stats_read": (_int, [_vp]),
+    "gh_debug_inject": (_int, [_int, _i64]),
+    "gh_debug_sort_stall": (_int, [_i64, _vp]),
 }
 
 
@@ -194,3 +199,17 @@ def tree_stats_read():
     call("gh_tree_stats_read", ctypes.addressof(out))
     return {"walks": out[0], "cell_steps": out[1], "target_visits": out[2], "interactions": out[3],
             "exact_tests": out[4], "leaf_interactions": out[5]}
+
+
+def inject(fault: int, count: int = 1) -> None:
+    """Host-side fault injection for tests: the next ``count`` occurrences of ``fault``
+    (GH_INJECT_ALLOC, GH_INJECT_TREE_WAIT) fail as if the device had reported them."""
+    call("gh_debug_inject", int(fault), int(count))
+
+
+def sort_stall(wait_ns: int):
+    """Runs the radix sort's look-back against a tile that is never published; returns
+    (status code, host nanoseconds the call took).  GH_ERR_TIMEOUT is the expected status."""
+    t = ctypes.c_int64(0)
+    rc = load().gh_debug_sort_stall(int(wait_ns), ctypes.addressof(t))
+    return int(rc), int(t.value)

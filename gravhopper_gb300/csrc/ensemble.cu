@@ -239,6 +239,15 @@ int ensemble_run(double* x, double* v, const double* mass, const int64_t* h_off,
   cudaStream_t ps = ws.stream;
   GH_CUDA_TRY(cudaEventRecord(ws.ev_in, st));
   GH_CUDA_TRY(cudaStreamWaitEvent(ps, ws.ev_in, 0));
+  // From here on every return, error or not, orders the caller's stream after the
+  // work already queued on the private stream (the next call reuses its buffers).
+  struct Rejoin {
+    cudaStream_t ps, st;
+    cudaEvent_t ev;
+    ~Rejoin() {
+      if (cudaEventRecord(ev, ps) == cudaSuccess) cudaStreamWaitEvent(st, ev, 0);
+    }
+  } rejoin{ps, st, ws.ev_out};
   GH_TRY(ensure(ws.sys, hs.size() * sizeof(EnsSys)));
   GH_TRY(ensure(ws.items, items.size() * sizeof(int2)));
   GH_TRY(ensure(ws.src[0], (size_t)ntot * sizeof(float4)));
@@ -285,8 +294,11 @@ int ensemble_run(double* x, double* v, const double* mass, const int64_t* h_off,
     int rc = GH_OK;
     for (int64_t k = 0; k < chunk && rc == GH_OK; k++) rc = launch(k, ps, true);
     cudaError_t ce = cudaStreamEndCapture(ps, &graph);
-    if (rc != GH_OK) return rc;
-    if (ce != cudaSuccess) return set_error(GH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    if (rc != GH_OK || ce != cudaSuccess) {
+      if (graph) cudaGraphDestroy(graph);
+      (void)cudaGetLastError();
+      return rc != GH_OK ? rc : set_error(GH_ERR_CUDA, "graph capture: %s", cudaGetErrorString(ce));
+    }
     ce = cudaGraphInstantiate(&exec, graph, 0);
     if (ce != cudaSuccess) {
       cudaGraphDestroy(graph);
@@ -304,9 +316,7 @@ int ensemble_run(double* x, double* v, const double* mass, const int64_t* h_off,
   prof_begin(ps);
   for (int64_t k = done; k < nsteps; k++) GH_TRY(launch(k - done, ps, false));
   prof_end(ps);
-  GH_CUDA_TRY(cudaEventRecord(ws.ev_out, ps));
-  GH_CUDA_TRY(cudaStreamWaitEvent(st, ws.ev_out, 0));
-  return GH_OK;
+  return GH_OK;  // `rejoin` orders the caller's stream after the steps
 }
 
 int ensemble_num_configs() { return kNumEnsConfigs; }

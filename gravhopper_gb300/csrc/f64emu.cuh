@@ -3,7 +3,7 @@
 //
 //     inv = RN( RN(1/s) / RN(sqrt(s)) )      (gravhopper/_jbgrav.c:166, :330)
 //
-// GB300 issues FP64 at 1/64 of the FP32 rate, and the two IEEE divisions and the
+// GB300 issues FP64 at 1/74 of the FP32 rate, and the two IEEE divisions and the
 // square root take more than half of the FP64 instructions of a pair.  Here the
 // three results are computed from the double's integer significand instead:
 //

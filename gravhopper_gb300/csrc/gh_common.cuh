@@ -102,6 +102,10 @@ struct Buffer {
 // Ensures `b` holds at least `bytes`; contents are not preserved on growth.
 int ensure(Buffer& b, size_t bytes);
 
+// Host-side fault injection for tests (gh_debug_inject): true, and one fewer pending,
+// when a fault of this kind is pending.
+bool inject_take(int fault);
+
 struct DeviceInfo {
   int device = -1;
   int num_sms = 0;

@@ -19,7 +19,12 @@ constexpr int64_t NOALLOC_MAX_N = 65536;
 // Kernel shape: 256 threads, 2 f32x2 packs (1024 targets per tile), 2 CTAs per SM.
 constexpr int NA_THREADS = 256, NA_P = 2, NA_MINB = 2;
 constexpr int NA_TILE = NA_THREADS * 2 * NA_P;
-constexpr int64_t NA_MAX_GRID = 304;  // persistent CTAs (2 per SM on a 152-SM GB300)
+// Bytes set aside for per-CTA partial sums (each CTA may leave partials for two tiles,
+// its first and its last).  The persistent grid is capped by what fits: 304 CTAs, i.e.
+// 2 per SM on a 152-SM GB300 (its occupancy).  A part with more SMs runs at most 304
+// CTAs here; the stream-K split still gives each of them an equal share of the pairs.
+constexpr size_t NA_PART_BUDGET = (size_t)304 * 2 * mixed_slot_floats(NA_THREADS, NA_P) * sizeof(float);
+constexpr int64_t NA_MAX_GRID = (int64_t)(NA_PART_BUDGET / (2 * mixed_slot_floats(NA_THREADS, NA_P) * sizeof(float)));
 constexpr int64_t NA_MAX_TILES = (NOALLOC_MAX_N + NA_TILE - 1) / NA_TILE;
 constexpr int NA_COM_THREADS = 256;
 
@@ -27,8 +32,7 @@ constexpr int NA_COM_THREADS = 256;
 constexpr size_t na_align(size_t b) { return (b + 255) & ~(size_t)255; }
 constexpr size_t NA_OFF_SRC = 0;
 constexpr size_t NA_OFF_PART = NA_OFF_SRC + na_align(NOALLOC_MAX_N * sizeof(float4));
-constexpr size_t NA_OFF_CNT =
-    NA_OFF_PART + na_align(2 * NA_MAX_GRID * mixed_slot_floats(NA_THREADS, NA_P) * sizeof(float));
+constexpr size_t NA_OFF_CNT = NA_OFF_PART + na_align(NA_PART_BUDGET);
 constexpr size_t NA_OFF_ORIGIN = NA_OFF_CNT + na_align(NA_MAX_TILES * sizeof(int));
 constexpr size_t NA_BYTES = NA_OFF_ORIGIN + na_align(4 * sizeof(double));  // about 16 MiB
 
@@ -75,18 +79,28 @@ __global__ void na_sources_kernel(const double* __restrict__ pos, const double* 
                        (float)dsub(pos[3 * i + 2], origin[2]), (float)mass[i]);
 }
 
-// Device address of the scratch array, looked up once per device.
+// Device address of the scratch array on each device.  Host code cannot use the
+// array's name as a device pointer, so the address comes from cudaGetSymbolAddress
+// with the device current.  It is looked up again on every call made outside stream
+// capture (a lookup is cheap), so a context torn down and re-created between calls
+// (cudaDeviceReset) never leaves a stale address behind; a call made during capture
+// uses the address of the last uncaptured call on that device, and the first call on a
+// device must come before any capture.
 static unsigned char* g_na_base[64];
 static std::mutex g_na_mu;
 
-static int na_scratch(int device, unsigned char** out) {
+static int na_scratch(int device, cudaStream_t st, unsigned char** out) {
   std::lock_guard<std::mutex> lk(g_na_mu);
-  if (!g_na_base[device]) {
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  GH_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+  if (cs == cudaStreamCaptureStatusNone) {
     void* p = nullptr;
     cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
     if (e != cudaSuccess || !p)
       return set_error(GH_ERR_CUDA, "cudaGetSymbolAddress(no-alloc scratch): %s", cudaGetErrorString(e));
     g_na_base[device] = (unsigned char*)p;
+  } else if (!g_na_base[device]) {
+    return set_error(GH_ERR_ARG, "gh_direct_mixed_noalloc: the first call on a device must not be captured");
   }
   *out = g_na_base[device];
   return GH_OK;
@@ -119,7 +133,7 @@ extern "C" int gh_direct_mixed_noalloc(const double* pos, const double* mass, in
   DeviceInfo di;
   GH_TRY(device_info(&di));
   unsigned char* base = nullptr;
-  GH_TRY(na_scratch(di.device, &base));
+  GH_TRY(na_scratch(di.device, st, &base));
   float4* src = (float4*)(base + NA_OFF_SRC);
   float* partials = (float*)(base + NA_OFF_PART);
   int* counters = (int*)(base + NA_OFF_CNT);

@@ -53,7 +53,25 @@ void prof_end(cudaStream_t st) {
   g_prof_open = nullptr;
 }
 
+// Pending injected faults, by kind (GH_INJECT_*).
+static std::atomic<long long> g_inject[3];
+
+bool inject_take(int fault) {
+  if (fault < 1 || fault > 2) return false;
+  long long k = g_inject[fault].load(std::memory_order_relaxed);
+  while (k > 0)
+    if (g_inject[fault].compare_exchange_weak(k, k - 1)) return true;
+  return false;
+}
+
 int ensure(Buffer& b, size_t bytes) {
+  if (bytes && inject_take(GH_INJECT_ALLOC)) {
+    // as a growth whose cudaMalloc ran out of memory: the old buffer is gone too
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+    return set_error(GH_ERR_OOM, "cudaMalloc(%zu bytes): out of memory (injected)", bytes);
+  }
   if (b.bytes >= bytes && b.ptr) return GH_OK;
   if (b.ptr) {
     cudaError_t e = cudaFree(b.ptr);
@@ -76,11 +94,14 @@ int ensure(Buffer& b, size_t bytes) {
 }
 
 int device_info(DeviceInfo* out) {
+  // Filled once per device under a lock: callers hold different engine locks, or none.
   static DeviceInfo cache[64];
+  static std::mutex mu;
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return set_error(GH_ERR_NO_DEVICE, "no CUDA device: %s", cudaGetErrorString(e));
   if (dev < 0 || dev >= 64) return set_error(GH_ERR_NO_DEVICE, "device index %d out of range", dev);
+  std::lock_guard<std::mutex> lk(mu);
   if (cache[dev].device != dev) {
     DeviceInfo d;
     d.device = dev;
@@ -102,6 +123,15 @@ const char* gh_last_error(void) { return gh::g_last_error; }
 int gh_version(void) { return GH_VERSION; }
 
 int64_t gh_launch_count(void) { return (int64_t)gh::g_launches.load(); }
+
+int gh_debug_inject(int fault, int64_t count) {
+  gh::clear_error();
+  if (fault != GH_INJECT_ALLOC && fault != GH_INJECT_TREE_WAIT)
+    return gh::set_error(GH_ERR_ARG, "unknown fault kind %d", fault);
+  if (count < 0) return gh::set_error(GH_ERR_ARG, "negative fault count");
+  gh::g_inject[fault].store(count);
+  return GH_OK;
+}
 
 int gh_kernel_timing(int enable) {
   std::lock_guard<std::mutex> lk(gh::g_prof_mu);

@@ -5,6 +5,9 @@
 // the tile's items, ranked in order within the warp (match-any per round of 32 items,
 // a warp-local running count per digit) and across warps by a prefix over the warps'
 // counts; across tiles from the tiles' ticket order.
+#include <chrono>
+#include <mutex>
+
 #include "sort.cuh"
 
 namespace gh {
@@ -50,18 +53,26 @@ __device__ __forceinline__ int64_t block_exclusive_scan_1024(int64_t v, int64_t*
 // which a CTA takes the next tile by ticket, counts its tile's digits, publishes them
 // and finds its output offsets by looking back over the earlier tiles' published
 // counts (decoupled look-back).  A CTA only ever waits on tiles with smaller tickets,
-// which are already running, and every wait is bounded (OS_MAX_SPINS, then the error
-// flag is set and the sort's result is garbage).
+// which are already running, and every wait is bounded: after wait_ns nanoseconds of
+// the GPU's global timer (OS_WAIT_NS in the sort; at most OS_MAX_SPINS polls either
+// way) the error flag is set, the wait ends and the sort's result is garbage, but
+// every write stays inside its buffers.
 // ---------------------------------------------------------------------------
 constexpr uint32_t OS_AGG = 1u << 30;    // status word: tile count published
 constexpr uint32_t OS_INC = 2u << 30;    // status word: inclusive prefix published
 constexpr uint32_t OS_VAL = (1u << 30) - 1;
 constexpr int OS_MAX_SPINS = 1 << 24;
+constexpr long long OS_WAIT_NS = 1000000000ll;  // one second
 constexpr int OS_MAX_PASSES = 8;        // 8-bit digits of one 64-bit word
 constexpr int OS_WIN = 8;               // predecessor tiles read per look-back step
 
 __device__ __forceinline__ uint32_t ld_status(const uint32_t* p) { return *(const volatile uint32_t*)p; }
 __device__ __forceinline__ void st_status(uint32_t* p, uint32_t v) { *(volatile uint32_t*)p = v; }
+__device__ __forceinline__ long long global_ns() {
+  long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
 
 // Digit counts of every pass of one key word: out[p*256 + d].
 __global__ void __launch_bounds__(RS_THREADS)
@@ -107,7 +118,7 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
     os_pass_kernel(const uint64_t* __restrict__ kin, const uint32_t* __restrict__ iin, uint64_t* __restrict__ kout,
                    uint32_t* __restrict__ iout, int words, int64_t n, int w, int shift,
                    const uint32_t* __restrict__ doff, uint32_t* __restrict__ status, int* __restrict__ ticket,
-                   int* __restrict__ err) {
+                   int* __restrict__ err, long long wait_ns) {
   // Blocked layout: warp wi owns the tile's items [wi*256, wi*256+256), lane l of it
   // item wi*256 + r*32 + l in round r.  A warp ranks its items by itself (match-any per
   // round and a warp-local running count per digit); one prefix over the warps per
@@ -181,13 +192,16 @@ __global__ void __launch_bounds__(RS_THREADS, 2)
       for (int j = 0; j < OS_WIN; j++) {
         if (done) break;
         const uint32_t* ps = status + (int64_t)(t0 - j) * RS_BINS + tid;
-        for (int spin = 0; (v[j] >> 30) == 0; spin++) {
-          if (spin >= OS_MAX_SPINS) {
-            atomicOr(err, 1);
-            v[j] = OS_INC;
-            break;
+        if ((v[j] >> 30) == 0) {
+          const long long w0 = global_ns();
+          for (int spin = 0; (v[j] >> 30) == 0; spin++) {
+            if (spin >= OS_MAX_SPINS || ((spin & 31) == 31 && global_ns() - w0 > wait_ns)) {
+              atomicOr(err, 1);
+              v[j] = OS_INC;  // give up: count the tile as empty
+              break;
+            }
+            v[j] = ld_status(ps);
           }
-          v[j] = ld_status(ps);
         }
         excl += v[j] & OS_VAL;
         done = (v[j] & ~OS_VAL) == OS_INC;
@@ -255,13 +269,13 @@ int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t*
     uint32_t* sq = status + (int64_t)q * tiles * RS_BINS;
     if (words == 1)
       os_pass_kernel<1><<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, dq, sq, tickets + q,
-                                                                err);
+                                                                err, OS_WAIT_NS);
     else if (words == 2)
       os_pass_kernel<2><<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, dq, sq, tickets + q,
-                                                                err);
+                                                                err, OS_WAIT_NS);
     else
       os_pass_kernel<0><<<(unsigned)tiles, RS_THREADS, 0, st>>>(ks, is, kd, id, words, n, w, shift, dq, sq, tickets + q,
-                                                                err);
+                                                                err, OS_WAIT_NS);
     GH_LAUNCH_CHECK();
     uint64_t* tk = ks;
     ks = kd;
@@ -274,6 +288,49 @@ int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t*
     GH_CUDA_TRY(cudaMemcpyAsync(keys, ks, sizeof(uint64_t) * words * n, cudaMemcpyDeviceToDevice, st));
     GH_CUDA_TRY(cudaMemcpyAsync(idx, is, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, st));
   }
+  return GH_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Test of the bounded wait (gh_debug_sort_stall): two tiles of zero keys; the
+// ticket counter starts at 1, so the only CTA takes tile 1 and looks back at tile 0,
+// which nothing publishes.  Its loads and stores stay inside the two tiles' buffers:
+// with the wait given up, tile 0 counts as empty and tile 1's keys go to positions
+// [0, RS_TILE).
+// ---------------------------------------------------------------------------
+struct StallWS {
+  Buffer keys, idx, scratch;
+};
+static StallWS g_stall[64];
+
+int sort_stall_test(int device, long long wait_ns, cudaStream_t st, int* gave_up) {
+  StallWS& ws = g_stall[device];
+  const int64_t n = 2 * RS_TILE, tiles = 2;
+  GH_TRY(ensure(ws.keys, 2 * n * sizeof(uint64_t)));
+  GH_TRY(ensure(ws.idx, 2 * n * sizeof(uint32_t)));
+  // digit offsets (256), tile status words (2 x 256), ticket, error flag
+  GH_TRY(ensure(ws.scratch, (RS_BINS * (1 + tiles) + 2) * sizeof(uint32_t)));
+  uint64_t* kin = (uint64_t*)ws.keys.ptr;
+  uint32_t* iin = (uint32_t*)ws.idx.ptr;
+  uint32_t* doff = (uint32_t*)ws.scratch.ptr;
+  uint32_t* status = doff + RS_BINS;
+  int* ticket = (int*)(status + tiles * RS_BINS);
+  int* err = ticket + 1;
+  GH_CUDA_TRY(cudaMemsetAsync(ws.keys.ptr, 0, ws.keys.bytes, st));
+  GH_CUDA_TRY(cudaMemsetAsync(ws.idx.ptr, 0, ws.idx.bytes, st));
+  GH_CUDA_TRY(cudaMemsetAsync(ws.scratch.ptr, 0, (RS_BINS * (1 + tiles) + 2) * sizeof(uint32_t), st));
+  GH_CUDA_TRY(cudaMemsetAsync(ticket, 1, 1, st));  // ticket = 1 (little-endian low byte)
+  os_hist_kernel<<<1, RS_THREADS, 0, st>>>(kin, n, 1, doff);
+  GH_LAUNCH_CHECK();
+  os_offsets_kernel<<<1, RS_BINS, 0, st>>>(doff, 1);
+  GH_LAUNCH_CHECK();
+  os_pass_kernel<1><<<1, RS_THREADS, 0, st>>>(kin, iin, kin + n, iin + n, 1, n, 0, 0, doff, status, ticket, err,
+                                              wait_ns);
+  GH_LAUNCH_CHECK();
+  int h = 0;
+  GH_CUDA_TRY(cudaMemcpyAsync(&h, err, sizeof(int), cudaMemcpyDeviceToHost, st));
+  GH_CUDA_TRY(cudaStreamSynchronize(st));
+  *gave_up = h;
   return GH_OK;
 }
 
@@ -346,3 +403,21 @@ int exclusive_scan_i32(const int* in, int* out, int64_t n, int* scratch, cudaStr
 }
 
 }  // namespace gh
+
+extern "C" int gh_debug_sort_stall(int64_t wait_ns, int64_t* waited_ns) {
+  using namespace gh;
+  clear_error();
+  if (wait_ns < 0 || wait_ns > 10000000000ll) return set_error(GH_ERR_ARG, "wait_ns must be in [0, 1e10]");
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lk(mu);
+  const auto t0 = std::chrono::steady_clock::now();
+  int gave_up = 0;
+  GH_TRY(sort_stall_test(di.device, (long long)wait_ns, nullptr, &gave_up));
+  if (waited_ns)
+    *waited_ns = (int64_t)std::chrono::duration_cast<std::chrono::nanoseconds>(std::chrono::steady_clock::now() - t0)
+                     .count();
+  if (gave_up) return set_error(GH_ERR_TIMEOUT, "radix sort look-back gave up after %lld ns", (long long)wait_ns);
+  return GH_OK;
+}

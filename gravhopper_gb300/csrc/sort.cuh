@@ -22,6 +22,10 @@ int64_t radix_scratch_words(int64_t n);
 int radix_sort_keys(uint64_t* keys, uint32_t* idx, uint64_t* keys_tmp, uint32_t* idx_tmp, int words,
                     int bits_per_word, int64_t n, uint32_t* scratch_u32, cudaStream_t st, int* err = nullptr);
 
+// Runs one sort pass whose look-back waits on a tile that is never published (see
+// sort.cu); *gave_up receives the error flag the bounded wait set.
+int sort_stall_test(int device, long long wait_ns, cudaStream_t st, int* gave_up);
+
 // Exclusive scan of in[0..n) into out[0..n] (out[n] = total).  `scratch` must hold
 // scan_scratch_ints(n) entries.  out may alias in.
 int64_t scan_scratch_ints(int64_t n);

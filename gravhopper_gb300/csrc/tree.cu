@@ -50,6 +50,7 @@ struct TreeRoot {
   double size;
   double inv;           // RN(1 / size)
   long long margin;     // 0: fast keys allowed; -1: the FP64 recurrence for every particle
+  int bad;              // a particle position or mass is NaN or infinite
 };
 
 // ---------------------------------------------------------------------------
@@ -58,16 +59,23 @@ struct TreeRoot {
 constexpr int BB_THREADS = 256;
 constexpr int BB_BLOCKS = 304;
 
+// Per block: the box (min xyz, max xyz) and whether any position or mass is not
+// finite (the reference's insert never terminates on such particles), 7 doubles.
+constexpr int BB_PART = 7;
+
 __global__ void __launch_bounds__(BB_THREADS)
-    bbox_partial_kernel(const double* __restrict__ pos, int64_t n, double* __restrict__ part) {
+    bbox_partial_kernel(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n,
+                        double* __restrict__ part) {
   __shared__ double s_mn[3][BB_THREADS], s_mx[3][BB_THREADS];
   double mn[3], mx[3];
-  bool have = false;
+  bool have = false, bad = false;
   for (int64_t i = (int64_t)blockIdx.x * BB_THREADS + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * BB_THREADS) {
+    bad = bad || !isfinite(mass[i]);
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       double q = pos[3 * i + k];
+      bad = bad || !isfinite(q);
       if (!have) {
         mn[k] = mx[k] = q;
       } else {
@@ -89,7 +97,7 @@ __global__ void __launch_bounds__(BB_THREADS)
     s_mn[k][threadIdx.x] = mn[k];
     s_mx[k][threadIdx.x] = mx[k];
   }
-  __syncthreads();
+  bad = __syncthreads_or(bad);
   for (int s = BB_THREADS / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
 #pragma unroll
@@ -104,9 +112,10 @@ __global__ void __launch_bounds__(BB_THREADS)
   if (threadIdx.x == 0) {
 #pragma unroll
     for (int k = 0; k < 3; k++) {
-      part[6 * blockIdx.x + k] = s_mn[k][0];
-      part[6 * blockIdx.x + 3 + k] = s_mx[k][0];
+      part[BB_PART * blockIdx.x + k] = s_mn[k][0];
+      part[BB_PART * blockIdx.x + 3 + k] = s_mx[k][0];
     }
+    part[BB_PART * blockIdx.x + 6] = bad ? 1.0 : 0.0;
   }
 }
 
@@ -129,12 +138,16 @@ __global__ void root_kernel(const double* __restrict__ part, int nb, double eps,
   const int lane = threadIdx.x;
   const double inf = __longlong_as_double(0x7ff0000000000000ll);
   double mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf};
-  for (int b = lane; b < nb; b += 32)
+  bool bad = false;
+  for (int b = lane; b < nb; b += 32) {
     for (int k = 0; k < 3; k++) {
-      const double a = part[6 * b + k], c = part[6 * b + 3 + k];
+      const double a = part[BB_PART * b + k], c = part[BB_PART * b + 3 + k];
       if (a < mn[k]) mn[k] = a;
       if (c > mx[k]) mx[k] = c;
     }
+    bad = bad || part[BB_PART * b + 6] != 0.0;
+  }
+  bad = __any_sync(0xffffffffu, bad);
   for (int o = 16; o > 0; o >>= 1)
     for (int k = 0; k < 3; k++) {
       const double a = __shfl_xor_sync(0xffffffffu, mn[k], o), c = __shfl_xor_sync(0xffffffffu, mx[k], o);
@@ -151,6 +164,7 @@ __global__ void root_kernel(const double* __restrict__ part, int nb, double eps,
     amax = fmax(amax, fabs(root->c[k]));
   }
   root->size = bs;
+  root->bad = bad ? 1 : 0;
   root->inv = ddiv(1.0, bs);
   root->margin = (bs > 0x1p-900 && bs < 0x1p+900 && amax < 0x1p+900) ? 0 : -1;
 }
@@ -797,7 +811,7 @@ struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
   Buffer nA, nC, nM, nF, parent, nchild, arrive, kids, xh[2];
   Buffer list;                // particle lists: key fallbacks, then cell openers
-  int* host_flags = nullptr;  // pinned: the 8 device flags, then nnodes
+  int* host_flags = nullptr;  // pinned: the 8 device flags, nnodes, the root's non-finite flag
   int words = TREE_MIN_WORDS;
   int64_t full_sort_n = -1;  // particle count whose last build needed the full multi-word sort
 };
@@ -829,11 +843,11 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   if (!ws.host_flags) GH_CUDA_TRY(cudaMallocHost((void**)&ws.host_flags, 16 * sizeof(int)));
   const int T = 256;
   // 1. root cell
-  GH_TRY(ensure(ws.part, BB_BLOCKS * 6 * sizeof(double)));
+  GH_TRY(ensure(ws.part, BB_BLOCKS * BB_PART * sizeof(double)));
   GH_TRY(ensure(ws.root, sizeof(TreeRoot)));
   int nb = (int)((n + BB_THREADS - 1) / BB_THREADS);
   if (nb > BB_BLOCKS) nb = BB_BLOCKS;
-  bbox_partial_kernel<<<nb, BB_THREADS, 0, st>>>(pos, n, (double*)ws.part.ptr);
+  bbox_partial_kernel<<<nb, BB_THREADS, 0, st>>>(pos, mass, n, (double*)ws.part.ptr);
   GH_LAUNCH_CHECK();
   root_kernel<<<1, 32, 0, st>>>((const double*)ws.part.ptr, nb, eps, (TreeRoot*)ws.root.ptr);
   GH_LAUNCH_CHECK();
@@ -883,6 +897,8 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
       tie_copy_kernel<<<gn, T, 0, st>>>(keys, words, n, idx, ktmp, itmp);
       GH_LAUNCH_CHECK();
     }
+    if (inject_take(GH_INJECT_TREE_WAIT))  // test hook: as if a look-back wait had run out
+      GH_CUDA_TRY(cudaMemsetAsync(flags + 5, 1, 1, st));
     lcp_kernel<<<gn1, T, 0, st>>>(keys, words, n, (int*)ws.lp.ptr, (int*)ws.flags.ptr);
     GH_LAUNCH_CHECK();
     count_kernel<<<gn, T, 0, st>>>((const int*)ws.lp.ptr, n, (int*)ws.cnt.ptr, (int*)ws.depth.ptr,
@@ -892,7 +908,14 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
     GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
     GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 8, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
                                 st));
+    GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 9, &root->bad, sizeof(int), cudaMemcpyDeviceToHost, st));
     GH_CUDA_TRY(cudaStreamSynchronize(st));
+    // The kernels so far index only by particle and sort slot, whatever the keys hold,
+    // so non-finite input is refused here, before any cell is built from it.
+    if (ws.host_flags[9])
+      return set_error(GH_ERR_ARG,
+                       "tree: particle positions and masses must be finite (the reference's octree insert "
+                       "does not terminate on NaN or infinite coordinates)");
     if (ws.host_flags[5]) return set_error(GH_ERR_TIMEOUT, "tree: radix sort look-back gave up");
     if (ws.host_flags[2] && !full_sort) {  // a long run of equal first words
       full_sort = true;

@@ -219,7 +219,7 @@ class Simulation(object):
                     pool = ThreadPoolExecutor(max_workers=1)
                     copy_stream = torch.cuda.Stream(device=dev)
                 ready = torch.cuda.Event()
-                ready.record()
+                ready.record(torch.cuda.current_stream(dev))
                 if pending is not None:
                     pending.result()
                 pending = pool.submit(self._copy_history, hp, hv, ready, copy_stream, t0 + done + 1)

@@ -112,10 +112,12 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
  * passes device inputs pos (np,3), mass (np) and the output acc (np,3); all scratch
  * lives in one fixed ~16 MiB array in this library's device memory, held by every GPU
  * that loads the library until the process exits.  np above 65536 is rejected with
- * GH_ERR_ARG.  The first call on a device looks up that array's device address (make
- * this first call before any stream capture).  Every call shares the array: calls
- * that overlap on the GPU (different streams, or threads) race and must not be
- * issued. */
+ * GH_ERR_ARG.  Each call made outside stream capture looks up that array's device
+ * address on the current device; a call during capture reuses the last one, so make
+ * the first call on a device before any stream capture.  The persistent grid is capped
+ * at 304 CTAs (two per SM of a 152-SM GB300) by the array's partial-sum space.  Every
+ * call shares the array and finds the previous call's contents in it: calls that
+ * overlap on the GPU (different streams, or threads) race and must not be issued. */
 int gh_direct_mixed_noalloc(const double* pos, const double* mass, int64_t np, double eps, double* acc,
                             void* stream);
 
@@ -218,6 +220,26 @@ int gh_tree_stats(int enable);
  * out[2] target cell visits, out[3] interactions, out[4] exact opening tests,
  * out[5] interactions with leaves. */
 int gh_tree_stats_read(int64_t* out);
+
+/* ---- fault injection for tests (no counterpart in the reference) ----------------- */
+
+/* Kinds of host-side fault that gh_debug_inject can make the library meet. */
+#define GH_INJECT_ALLOC 1     /* a device workspace allocation runs out of memory */
+#define GH_INJECT_TREE_WAIT 2 /* a tree build finds its radix sort's bounded wait given up */
+
+/* Makes the next `count` occurrences of `fault` fail on the host as if the device had
+ * reported them (0 clears it): GH_INJECT_ALLOC fails workspace reservations with
+ * GH_ERR_OOM (the reserved buffer is released, as after a failed growth);
+ * GH_INJECT_TREE_WAIT makes tree builds return GH_ERR_TIMEOUT after their sort.  Every
+ * later call works normally.  For testing the error paths; no GPU fault is involved. */
+int gh_debug_inject(int fault, int64_t count);
+
+/* Runs one pass of the tree build's radix sort over two tiles of keys in which tile 0
+ * is never published, so tile 1's bounded look-back wait gives up after wait_ns
+ * nanoseconds (GPU global timer) and sets the sort's error flag.  Returns GH_ERR_TIMEOUT
+ * when the wait gave up, as it must; *waited_ns, when non-NULL, receives the host time
+ * the call took.  Tests the bound without a hang. */
+int gh_debug_sort_stall(int64_t wait_ns, int64_t* waited_ns);
 
 #ifdef __cplusplus
 }

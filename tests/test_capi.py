@@ -49,3 +49,12 @@ def test_library_targets_sm_103a():
     from gravhopper_gb300 import _build
     assert "arch=compute_103a,code=sm_103a" in " ".join(_build.ARCH)
     assert os.path.exists(_build.LIB)
+
+
+def test_fault_injection_arguments_without_gpu(lib):
+    """The test-only fault hooks validate their arguments on the host (no device use)."""
+    assert lib.gh_debug_inject(99, 1) == _capi.GH_ERR_ARG
+    assert lib.gh_debug_inject(_capi.GH_INJECT_ALLOC, -1) == _capi.GH_ERR_ARG
+    assert lib.gh_debug_inject(_capi.GH_INJECT_ALLOC, 0) == _capi.GH_OK
+    assert lib.gh_debug_inject(_capi.GH_INJECT_TREE_WAIT, 0) == _capi.GH_OK
+    assert lib.gh_debug_sort_stall(-1, None) == _capi.GH_ERR_ARG

@@ -4,25 +4,31 @@ gh_direct_mixed_noalloc is for callers that cannot let the library allocate devi
 memory (an application that owns all device memory through its own pool, or a
 stepping loop that must not call cudaMalloc/cudaFree because they can synchronise the
 device).  Its scratch is a fixed array inside the library, so this checks two calls
-in a row against the allocating entry point gh_direct_dev (mixed precision), within
-the mixed form's tolerance, and that sizes beyond the fixed limit are refused.
-Collected last so that a stop-at-first-failure run has run every other test first.
+in a row against the allocating entry point gh_direct_dev (mixed precision) and
+against the FP64 oracle, within the mixed form's tolerance, with softening and with
+eps = 0 (the variant that gives a coincident pair no term), and that sizes beyond the
+fixed limit are refused.  Collected last so that a stop-at-first-failure run has run
+every other test first.
 """
 import numpy as np
 import pytest
 
+from oracle import oracle
+
 pytestmark = pytest.mark.gpu
 
 MIXED_RMS_TOL = 1e-6
+MIXED_MAX_TOL = 1e-3
 NOALLOC_MAX_N = 65536
 
 
-def _rel_rms(a, b):
+def _rel(a, b):
     r = np.linalg.norm(a - b, axis=1) / np.linalg.norm(b, axis=1)
-    return float(np.sqrt(np.mean(r * r)))
+    return float(np.sqrt(np.mean(r * r))), float(r.max())
 
 
-def test_no_alloc_matches_allocating_entry_point(lib, cuda):
+@pytest.mark.parametrize("eps", [5e-5, 0.0])
+def test_no_alloc_matches_allocating_entry_point_and_oracle(lib, cuda, eps):
     import torch
 
     from gravhopper_gb300 import _capi, ics
@@ -32,15 +38,18 @@ def test_no_alloc_matches_allocating_entry_point(lib, cuda):
         m = torch.from_numpy(ic["mass"]).to(cuda)
         stream = torch.cuda.current_stream().cuda_stream
         ref = torch.empty((n, 3), dtype=torch.float64, device=cuda)
-        _capi.check(lib.gh_direct_dev(x.data_ptr(), m.data_ptr(), n, None, 0, 5e-5, _capi.GH_PREC_MIXED,
+        _capi.check(lib.gh_direct_dev(x.data_ptr(), m.data_ptr(), n, None, 0, eps, _capi.GH_PREC_MIXED,
                                       ref.data_ptr(), stream))
         ref_h = ref.cpu().numpy()
+        exact = oracle.direct_summation(ic["pos"], ic["mass"], eps)
         for call in range(2):
             out = torch.full((n, 3), float("nan"), dtype=torch.float64, device=cuda)
-            _capi.check(lib.gh_direct_mixed_noalloc(x.data_ptr(), m.data_ptr(), n, 5e-5, out.data_ptr(), stream))
+            _capi.check(lib.gh_direct_mixed_noalloc(x.data_ptr(), m.data_ptr(), n, eps, out.data_ptr(), stream))
             got = out.cpu().numpy()
-            assert np.isfinite(got).all(), (n, call)
-            assert _rel_rms(got, ref_h) <= MIXED_RMS_TOL, (n, call)
+            assert np.isfinite(got).all(), (n, eps, call)
+            assert _rel(got, ref_h)[0] <= MIXED_RMS_TOL, (n, eps, call)
+            rms, mx = _rel(got, exact)
+            assert rms <= MIXED_RMS_TOL and mx <= MIXED_MAX_TOL, (n, eps, call, rms, mx)
 
 
 def test_no_alloc_refuses_oversize(lib, cuda):
