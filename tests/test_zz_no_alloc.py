@@ -4,10 +4,10 @@ gh_direct_mixed_noalloc is for callers that cannot let the library allocate devi
 memory (an application that owns all device memory through its own pool, or a
 stepping loop that must not call cudaMalloc/cudaFree because they can synchronise the
 device).  Its scratch is a fixed array inside the library, so this checks two calls
-in a row against the allocating entry point gh_direct_dev (mixed precision) and
-against the FP64 oracle, within the mixed form's tolerance, with softening and with
-eps = 0 (the variant that gives a coincident pair no term), and that sizes beyond the
-fixed limit are refused.  Collected last so that a stop-at-first-failure run has run
+in a row against the allocating entry point gh_direct_dev (mixed precision, within
+1e-6) and against the FP64 oracle, within the mixed form's tolerance (rms 1e-6 with
+softening, 1e-5 with eps = 0, the variant that gives a coincident pair no term), and
+that sizes beyond the fixed limit are refused.  Collected last so that a stop-at-first-failure run has run
 every other test first.
 """
 import numpy as np
@@ -19,6 +19,9 @@ pytestmark = pytest.mark.gpu
 
 MIXED_RMS_TOL = 1e-6
 MIXED_MAX_TOL = 1e-3
+# Without softening the closest pairs' FP32 offsets dominate their forces; the mixed
+# form's stated tolerance against FP64 there is rms 1e-5 (as for the other eps = 0 tests).
+MIXED_RMS_TOL_EPS0 = 1e-5
 NOALLOC_MAX_N = 65536
 
 
@@ -49,7 +52,8 @@ def test_no_alloc_matches_allocating_entry_point_and_oracle(lib, cuda, eps):
             assert np.isfinite(got).all(), (n, eps, call)
             assert _rel(got, ref_h)[0] <= MIXED_RMS_TOL, (n, eps, call)
             rms, mx = _rel(got, exact)
-            assert rms <= MIXED_RMS_TOL and mx <= MIXED_MAX_TOL, (n, eps, call, rms, mx)
+            tol = MIXED_RMS_TOL if eps > 0 else MIXED_RMS_TOL_EPS0
+            assert rms <= tol and mx <= MIXED_MAX_TOL, (n, eps, call, rms, mx)
 
 
 def test_no_alloc_refuses_oversize(lib, cuda):
