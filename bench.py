@@ -24,7 +24,10 @@ Also reported on the same line:
   host cores, on a bounded sample of targets.
 
 ``--impl reference`` times that CPU implementation alone on the same metric.
-Under torchrun with N > 1, every rank runs its own system (replicas; weak scaling).
+Under torchrun with N > 1, every rank runs its own system (replicas; weak scaling);
+with ``--shard targets`` the ranks split one system by target and all-gather the
+half-drifted positions every step (strong scaling; the mixed form overlaps the gather
+with the force of the rank's own particles).
 """
 from __future__ import annotations
 
@@ -55,6 +58,9 @@ def parse():
     ap.add_argument("--n", type=int, default=1 << 20)
     ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
     ap.add_argument("--no-secondary", action="store_true")
+    ap.add_argument("--shard", default="replicas", choices=["replicas", "targets"],
+                    help="N>1: one system per rank (weak scaling) or one system split by target "
+                         "over the ranks, positions all-gathered each step (strong scaling)")
     ap.add_argument("--cpu-targets", type=int, default=49152,
                     help="targets in the CPU-baseline sample (each against all N sources)")
     ap.add_argument("--report", choices=["config0", "config1", "config2", "config3", "config4"],
@@ -160,11 +166,13 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def _config(args):
+def _config(args, world=1):
+    shard = getattr(args, "shard", "replicas") == "targets"
     return {"workload": f"direct-sum DKD leapfrog step, Plummer sphere N={args.n} (b=1 pc, M=1e6 Msun, "
                         f"eps=0.05 pc, dt=0.005 Myr)",
             "precision": args.precision, "n": args.n, "pairs_per_step": args.n * (args.n - 1),
-            "l2": "flushed (256 MB write) before every timed step", "parallelism": "replicas"}
+            "l2": "flushed (256 MB write) before every timed step",
+            "parallelism": f"targets split over {world} ranks" if shard else "replicas"}
 
 
 def main():
@@ -193,7 +201,8 @@ def main():
         dist.init_process_group("nccl", device_id=dev)
     _capi.load()
     n = args.n
-    ic = ics.plummer(n, seed=rank)
+    shard = args.shard == "targets"
+    ic = ics.plummer(n, seed=0 if shard else rank)
     x = torch.from_numpy(ic["pos"]).to(dev)
     v = torch.from_numpy(ic["vel"]).to(dev)
     m = torch.from_numpy(ic["mass"]).to(dev)
@@ -209,6 +218,24 @@ def main():
 
     def step():
         engine.run_dkd(x, v, m, 1, dt, eps, algorithm="direct", precision=args.precision)
+
+    if shard:
+        # one system split by target: this rank's slice, all masses, positions gathered per step
+        from gravhopper_gb300 import sharding
+        counts = sharding.counts_of(n, world)
+        lo_, hi_ = sharding.target_slices(n, world)[rank]
+        x = x[lo_:hi_].contiguous()
+        v = v[lo_:hi_].contiguous()
+
+        def step():  # noqa: F811
+            sharding.run_dkd_sharded(x, v, m, counts, 1, dt, eps, precision=args.precision)
+
+    tuned = None
+    if args.precision == "mixed" and not shard:
+        # the tile shape of this size's fused step, picked by timing every shape (untimed here)
+        from gravhopper_gb300 import autotune
+        best, ms = autotune.tune_direct(sizes=(n,), kinds=("step",), device=dev)["step"][n]
+        tuned = {"shape": best, "ms_per_step_by_shape": {k: round(t, 2) for k, t in ms.items()}}
 
     for _ in range(args.warmup):
         step()
@@ -227,6 +254,9 @@ def main():
         barrier()
     launches = _capi.launch_count() - launches0
     _capi.kernel_timing(False)
+    if tuned is not None:
+        from gravhopper_gb300 import autotune
+        autotune.clear_direct()  # the other measurements use the library's own size table
     kern_ms, kern_n = _capi.kernel_timing_collect()
     step_ms = sum(a.elapsed_time(b) for a, b in ev)
     t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
@@ -234,7 +264,7 @@ def main():
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
     step_ms_max = float(t.item())
     pairs = float(n) * (n - 1)
-    value = world * pairs * args.steps / (step_ms_max * 1e-3) / 1e9
+    value = (1 if shard else world) * pairs * args.steps / (step_ms_max * 1e-3) / 1e9
 
     # End to end through the host-buffer C ABI (pinned host memory, copies timed).
     hp = torch.from_numpy(ic["pos"]).pin_memory()
@@ -255,7 +285,8 @@ def main():
            "h2d_bytes_per_step": n * 3 * 8 + n * 8, "d2h_bytes_per_step": n * 3 * 8}
 
     kern_avg_s = kern_ms / max(kern_n, 1) * 1e-3
-    achieved = pairs / kern_avg_s / 1e9
+    # pairs one force launch evaluates (sharded: this rank's targets, own and others' sources)
+    achieved = (pairs if not shard else float(x.shape[0]) * n * args.steps / max(kern_n, 1)) / kern_avg_s / 1e9
     mixed = args.precision == "mixed"
     # mixed: 12 FP32 FMA-pipe lane-ops per pair; FP64: the 12 of the reference's pair
     # operations that stay on the FP64 pipe (squared distance, division and square
@@ -284,9 +315,10 @@ def main():
         # long detail first, the headline extras last (a reader of the line's tail sees them)
         line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": step_ms_max / args.steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None,
+                "scaling": "strong" if shard else "weak", "vs_baseline": None,
                 "dtype": "f32" if args.precision == "mixed" else "f64",
-                "data": "synthetic", "config": _config(args), "roofline": roofline,
+                "data": "synthetic", "config": {**_config(args, world), "tile_autotune": tuned},
+                "roofline": roofline,
                 "clocks": clocks.summary(), "e2e": e2e, "gpu_launches": launches,
                 "secondary": _rounded(secondary)}
         if secondary.get("tree"):
@@ -679,8 +711,10 @@ def report_config3(dev, steps=1000, loop_steps=20):
 
 def report_config4(dev, n=16384):
     """Adjoint gradients with respect to x0 against FP64 central finite differences
-    (FP64 rollouts, N = 16,384): 64 random coordinates over 20 steps, and 8 over the
-    full 200-step rollout with checkpoints every 20 steps."""
+    (FP64 rollouts, N = 16,384): 64 random coordinates over 20 steps, and 64 over the
+    full 200-step rollout with checkpoints every 20 steps, where the differences at
+    h = 3e-10, 1e-10, 3e-11 kpc are also extrapolated twice (Richardson: the h^2 and
+    h^4 terms cancel)."""
     import numpy as np
     import torch
 
@@ -691,7 +725,7 @@ def report_config4(dev, n=16384):
     v0 = torch.from_numpy(ic["vel"]).to(dev)
     m = torch.from_numpy(ic["mass"]).to(dev)
     out = {"n": n}
-    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (200, 8, 20, (1e-9, 1e-11, 1e-12))):
+    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (200, 64, 20, (3e-10, 1e-10, 3e-11))):
         rng = np.random.default_rng(1)
         xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
         vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()
@@ -709,6 +743,8 @@ def report_config4(dev, n=16384):
         idx = rng.choice(3 * n, size=ncoord, replace=False)
         flat = x0.reshape(-1)
         row = {"coordinates": ncoord, "checkpoint_every": ckpt}
+        den = np.maximum(np.abs(g[idx]), 1e-3 * np.abs(g).max())
+        fds = []
         for h in hs:
             fd = []
             for i in idx:
@@ -717,8 +753,16 @@ def report_config4(dev, n=16384):
                 xm[i] -= h
                 fd.append((loss_at(xp) - loss_at(xm)) / (2 * h))
             fd = np.array(fd)
-            rel = np.abs(fd - g[idx]) / np.maximum(np.abs(g[idx]), 1e-3 * np.abs(g).max())
+            fds.append(fd)
+            rel = np.abs(fd - g[idx]) / den
             row[f"h_{h:g}"] = {"rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel))}
+        if len(hs) == 3:
+            r = hs[0] / hs[1]
+            r1 = [(r * r * fds[k + 1] - fds[k]) / (r * r - 1) for k in range(2)]
+            r2 = (r ** 4 * r1[1] - r1[0]) / (r ** 4 - 1)
+            rel = np.abs(r2 - g[idx]) / den
+            row["richardson_2"] = {"rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
+                                   "rel_err_per_coordinate": [float(f"{e:.3g}") for e in rel]}
         out[f"steps_{steps}"] = row
     return out
 

@@ -85,6 +85,8 @@ SIGNATURES = {
     "gh_dkd_backward_dev": (_int, [_vp, _vp, _vp, _i64, _i64, _dbl, _dbl, _int, _vp, _vp, _vp, _vp]),
     "gh_dkd_backward_chain_dev": (_int, [_vp, _vp, _vp, _i64, _vp, _i64, _dbl, _dbl, _int, _vp, _vp, _vp, _vp]),
     "gh_direct_num_shapes": (_int, []),
+    "gh_direct_tune": (_int, [_i64, _int, _int]),
+    "gh_direct_shape_for": (_int, [_i64, _int]),
     "gh_direct_set_fp64_form": (_int, [_int]),
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),

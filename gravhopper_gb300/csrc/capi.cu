@@ -194,6 +194,17 @@ int gh_direct_set_shape(int shape) {
 
 int gh_direct_num_shapes(void) { return kNumMixedShapes; }
 
+int gh_direct_tune(int64_t n_min, int fused_step, int shape) {
+  clear_error();
+  return tune_rule(n_min, fused_step, shape);
+}
+
+int gh_direct_shape_for(int64_t n, int fused_step) {
+  clear_error();
+  if (n < 0 || (fused_step != 0 && fused_step != 1)) return -1;
+  return shape_for(n, fused_step);
+}
+
 int gh_direct_set_fp64_form(int form) {
   clear_error();
   return set_f64_form(form);

@@ -108,8 +108,36 @@ static int g_f64_form = -1;  // -1 by target count, 0 thread per target, 1 order
 // every size (e.g. 1.78 ms against 1.93 ms for the packed 128 x 4 at N = 65,536) and
 // for the leapfrog step up to ~128k, 384 threads x 6 targets for larger steps, whose
 // heavier epilogue favours it (435 ms per step at N = 1M against 443 ms).
+//
+// An autotuner can replace that table (gh_direct_tune): per epilogue kind (force or
+// fused leapfrog step), rules "from n_min particles on, shape k"; the rule with the
+// largest n_min <= n applies, and sizes below every rule fall back to the table.
+constexpr int kMaxTuneRules = 32;
+struct TuneRule {
+  int64_t n_min;
+  int shape;
+};
+static TuneRule g_tune[2][kMaxTuneRules];
+static int g_ntune[2] = {0, 0};
+static std::mutex g_tune_mu;
+
+static int tuned_shape(int64_t n, bool dkd) {
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  const int k = dkd ? 1 : 0;
+  int best = -1;
+  int64_t best_min = -1;
+  for (int r = 0; r < g_ntune[k]; r++)
+    if (g_tune[k][r].n_min <= n && g_tune[k][r].n_min > best_min) {
+      best_min = g_tune[k][r].n_min;
+      best = g_tune[k][r].shape;
+    }
+  return best;
+}
+
 static int auto_shape(int64_t np, int64_t nt, bool dkd) {
   const int64_t n = np > nt ? np : nt;
+  const int tuned = tuned_shape(n, dkd);
+  if (tuned >= 0) return tuned;
   if (n < 12288) return 7;                   // packed, 256 threads, 1 pack, 4 CTAs/SM
   if (n < 24576) return 3;                   // packed, 128 threads, 2 packs, 4 CTAs/SM
   if (dkd && n >= (1 << 17)) return 12;      // scalar, 384 threads x 6 targets
@@ -198,6 +226,31 @@ int set_f64_form(int form) {
   if (form < -1 || form > 1) return set_error(GH_ERR_ARG, "fp64 form %d out of range", form);
   g_f64_form = form;
   return GH_OK;
+}
+
+int tune_rule(int64_t n_min, int fused_step, int shape) {
+  if (fused_step != 0 && fused_step != 1) return set_error(GH_ERR_ARG, "fused_step must be 0 or 1");
+  if (shape >= kNumMixedShapes) return set_error(GH_ERR_ARG, "mixed shape %d out of range", shape);
+  std::lock_guard<std::mutex> lk(g_tune_mu);
+  if (shape < 0) {  // clear this kind's rules
+    g_ntune[fused_step] = 0;
+    return GH_OK;
+  }
+  if (n_min < 0) return set_error(GH_ERR_ARG, "n_min must be >= 0");
+  TuneRule* t = g_tune[fused_step];
+  for (int r = 0; r < g_ntune[fused_step]; r++)
+    if (t[r].n_min == n_min) {
+      t[r].shape = shape;
+      return GH_OK;
+    }
+  if (g_ntune[fused_step] >= kMaxTuneRules) return set_error(GH_ERR_ARG, "at most %d tuning rules", kMaxTuneRules);
+  t[g_ntune[fused_step]++] = TuneRule{n_min, shape};
+  return GH_OK;
+}
+
+int shape_for(int64_t n, int fused_step) {
+  if (g_mixed_shape >= 0) return g_mixed_shape;
+  return auto_shape(n, n, fused_step != 0);
 }
 
 int set_mixed_shape(int shape) {

@@ -13,6 +13,9 @@ int direct_force(const double* pos, const double* mass, int64_t np, const double
 
 // Selects the tile shape of the mixed direct kernel (index into kMixedShapes).
 int set_mixed_shape(int shape);
+// Autotuned shape rules (gh_direct_tune) and the shape a size would get.
+int tune_rule(int64_t n_min, int fused_step, int shape);
+int shape_for(int64_t n, int fused_step);
 int set_f64_form(int form);
 
 // `nsteps` leapfrog steps with the direct force, one fused launch per step.

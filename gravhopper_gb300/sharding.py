@@ -10,6 +10,8 @@ Two decompositions:
   compute the forces on their own slice against every source.  ``sharded_dkd`` is
   that loop; with the FP64 force it is bit-identical to the single-GPU run, because
   the position-mode sum adds an exact zero for a particle's own term.
+  ``run_dkd_sharded`` is the engine entry: in the mixed form it overlaps the
+  all-gather with the force of the rank's own particles, then adds the others'.
 
 The Barnes-Hut path would need a distributed tree and is run as replicas only.
 """
@@ -70,6 +72,62 @@ def sharded_dkd(x_local, v_local, mass_all, counts, nsteps, dt, eps, force_fn, g
     return x_local, v_local
 
 
+def run_dkd_sharded(x_local, v_local, mass_all, counts, nsteps, dt, eps, precision="mixed", group=None,
+                    force_fn=None):
+    """Drift-kick-drift steps of one direct-sum system split by target over the ranks.
+
+    Rank r owns particles [sum(counts[:r]), sum(counts[:r+1])) of the system (x_local,
+    v_local in kpc, km/s, updated in place; mass_all all masses in rank order).  Each
+    step all-gathers the half-drifted positions (N*24 bytes).
+
+    * ``precision="mixed"``: the all-gather runs asynchronously while this rank sums the
+      force of its own particles on its own targets; then the other ranks' particles
+      are added.  Each part is a compensated FP32 sum; the two are added in FP64.
+    * ``precision="fp64"``: one pass over all sources in ascending order after the
+      gather, so the result is the reference's bits (gravhopper/_jbgrav.c:299-353 with
+      the self pair's exact zero), the same as ``sharded_dkd``.
+
+    ``force_fn(sources, masses, eps, targets)`` defaults to the GPU direct sum in
+    ``precision``.  The step arithmetic is gravhopper/gravhopper.py:405-416.
+    """
+    import torch.distributed as dist
+    force_fn = force_fn or gpu_force_fn(precision)
+    world = dist.get_world_size(group) if dist.is_initialized() else 1
+    rank = dist.get_rank(group) if dist.is_initialized() else 0
+    if len(counts) != world:
+        raise ValueError("one particle count per rank is needed")
+    start = sum(counts[:rank])
+    n_local = counts[rank]
+    m_local = mass_all[start:start + n_local].contiguous()
+    m_remote = torch.cat([mass_all[:start], mass_all[start + n_local:]]).contiguous()
+    width = max(counts) if counts else 0
+    for _ in range(int(nsteps)):
+        xh = x_local + ((0.5 * v_local) * dt) * KMS_MYR_TO_KPC
+        if world == 1:
+            acc = force_fn(xh, mass_all, eps, xh)
+        else:
+            buf = torch.zeros((width, 3), dtype=xh.dtype, device=xh.device)
+            buf[:n_local] = xh
+            parts = [torch.empty_like(buf) for _ in counts]
+            work = dist.all_gather(parts, buf, group=group, async_op=True)
+            if precision == "fp64":
+                work.wait()
+                xh_all = torch.cat([p[:c] for p, c in zip(parts, counts)])
+                acc = force_fn(xh_all, mass_all, eps, xh)
+            else:
+                acc = force_fn(xh, m_local, eps, xh)  # overlaps the all-gather
+                work.wait()
+                others = [p[:c] for r, (p, c) in enumerate(zip(parts, counts)) if r != rank]
+                if m_remote.shape[0]:
+                    acc = acc + force_fn(torch.cat(others), m_remote, eps, xh)
+        acc = acc * ACCEL_UNIT
+        v_new = v_local + acc * dt
+        x_new = xh + ((0.5 * v_new) * dt) * KMS_MYR_TO_KPC
+        v_local.copy_(v_new)
+        x_local.copy_(x_new)
+    return x_local, v_local
+
+
 def gpu_force_fn(precision="fp64"):
     """Position-mode direct force on the GPU, for ``sharded_dkd``."""
     from . import engine
@@ -84,4 +142,4 @@ def counts_of(n, world):
     return [b - a for a, b in target_slices(n, world)]
 
 
-__all__ = ["partition_systems", "target_slices", "sharded_dkd", "gpu_force_fn", "counts_of"]
+__all__ = ["partition_systems", "target_slices", "sharded_dkd", "run_dkd_sharded", "gpu_force_fn", "counts_of"]

@@ -127,6 +127,17 @@ int gh_direct_mixed_noalloc(const double* pos, const double* mass, int64_t np, d
 int gh_direct_set_shape(int shape);
 int gh_direct_num_shapes(void);
 
+/* Installs an autotuned shape rule for the mixed-precision direct kernel (no
+ * counterpart in the reference): from n_min particles on (the rule with the largest
+ * n_min <= N applies), calls of kind fused_step (0 a force, 1 a fused leapfrog step)
+ * use tile shape `shape`; shape -1 clears that kind's rules.  Sizes below every rule
+ * keep the built-in table.  gh_direct_set_shape(k >= 0) overrides the rules. */
+int gh_direct_tune(int64_t n_min, int fused_step, int shape);
+
+/* The tile shape a call of N particles of kind fused_step would use now (-1 on bad
+ * arguments); no device work. */
+int gh_direct_shape_for(int64_t n, int fused_step);
+
 /* Selects the FP64 direct kernel for all later calls in this process: 0 one thread
  * per target, 1 CTA-wide pair terms summed in order per target (for few targets),
  * -1 (the default) by target count.  Both give the reference's bits.  No counterpart

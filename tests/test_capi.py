@@ -58,3 +58,27 @@ def test_fault_injection_arguments_without_gpu(lib):
     assert lib.gh_debug_inject(_capi.GH_INJECT_ALLOC, 0) == _capi.GH_OK
     assert lib.gh_debug_inject(_capi.GH_INJECT_TREE_WAIT, 0) == _capi.GH_OK
     assert lib.gh_debug_sort_stall(-1, None) == _capi.GH_ERR_ARG
+
+
+def test_direct_tune_rules_without_gpu(lib):
+    """Autotuned shape rules: the rule with the largest n_min <= N applies per kind,
+    below every rule the built-in table does, and -1 clears the kind's rules."""
+    nshape = lib.gh_direct_num_shapes()
+    base_force = [lib.gh_direct_shape_for(n, 0) for n in (1000, 50000, 2000000)]
+    base_step = [lib.gh_direct_shape_for(n, 1) for n in (1000, 50000, 2000000)]
+    try:
+        assert lib.gh_direct_tune(10000, 0, 2) == _capi.GH_OK
+        assert lib.gh_direct_tune(100000, 0, 5) == _capi.GH_OK
+        assert lib.gh_direct_shape_for(1000, 0) == base_force[0]
+        assert lib.gh_direct_shape_for(10000, 0) == 2
+        assert lib.gh_direct_shape_for(99999, 0) == 2
+        assert lib.gh_direct_shape_for(2000000, 0) == 5
+        assert [lib.gh_direct_shape_for(n, 1) for n in (1000, 50000, 2000000)] == base_step
+        assert lib.gh_direct_tune(100000, 0, 6) == _capi.GH_OK  # replaces the rule
+        assert lib.gh_direct_shape_for(2000000, 0) == 6
+        assert lib.gh_direct_tune(0, 0, nshape) == _capi.GH_ERR_ARG
+        assert lib.gh_direct_tune(0, 2, 1) == _capi.GH_ERR_ARG
+        assert lib.gh_direct_shape_for(-1, 0) == -1
+    finally:
+        assert lib.gh_direct_tune(0, 0, -1) == _capi.GH_OK
+    assert [lib.gh_direct_shape_for(n, 0) for n in (1000, 50000, 2000000)] == base_force
