@@ -711,10 +711,10 @@ def report_config3(dev, steps=1000, loop_steps=20):
 
 def report_config4(dev, n=16384):
     """Adjoint gradients with respect to x0 against FP64 central finite differences
-    (FP64 rollouts, N = 16,384): 64 random coordinates over 20 steps, and 64 over the
-    full 200-step rollout with checkpoints every 20 steps, where the differences at
-    h = 3e-10, 1e-10, 3e-11 kpc are also extrapolated twice (Richardson: the h^2 and
-    h^4 terms cancel)."""
+    (FP64 rollouts, N = 16,384, 64 random coordinates each): over 20 steps, over 100
+    steps with checkpoints every 20, and over the full 200-step rollout with
+    checkpoints every 20, where the differences at h = 3e-10, 1e-10, 3e-11 kpc are also
+    extrapolated twice (Richardson: the h^2 and h^4 terms cancel)."""
     import numpy as np
     import torch
 
@@ -725,7 +725,8 @@ def report_config4(dev, n=16384):
     v0 = torch.from_numpy(ic["vel"]).to(dev)
     m = torch.from_numpy(ic["mass"]).to(dev)
     out = {"n": n}
-    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (200, 64, 20, (3e-10, 1e-10, 3e-11))):
+    for steps, ncoord, ckpt, hs in ((20, 64, 5, (1e-9,)), (100, 64, 20, (3e-10,)),
+                                    (200, 64, 20, (3e-10, 1e-10, 3e-11))):
         rng = np.random.default_rng(1)
         xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
         vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()

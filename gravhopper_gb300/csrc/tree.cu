@@ -17,11 +17,12 @@
 //      particle and whose parent holds at least two, single-child chains included)
 //      laid out in depth-first preorder with skip ("next") indices and parent links,
 //      from the common prefix lengths of neighbouring keys;
-//   5. monopole pass, one launch bottom-up: leaves take the particle's position and
-//      mass exactly (gravoct_finalize, _jbgrav.c:467-483); the last child to finish
-//      sums its cell's children's mass and first moment (the reference sums per
-//      particle in insertion order, so the last bits of an internal COM can differ)
-//      and divides.
+//   5. monopoles: leaves take the particle's position and mass exactly
+//      (gravoct_finalize, _jbgrav.c:467-483); a cell holds a contiguous range of the
+//      key-ordered particles, so its mass and first moment are differences of exact
+//      192-bit fixed-point prefix sums, rounded to FP64 once (the reference rounds
+//      after every particle it adds, in insertion order, so the last bits of an
+//      internal COM can differ), and the centre of mass is first moment over mass.
 // Walk: one warp per 32 consecutive targets in key order.  Each lane applies the
 // reference's test "leaf or size/|center - x| < theta" (_jbgrav.c:496-502) to every
 // cell its own traversal reaches; the warp visits the union of those cells in
@@ -35,6 +36,7 @@
 
 #include "direct.cuh"
 #include "engine.h"
+#include "fixed192.cuh"
 #include "sort.cuh"
 
 namespace gh {
@@ -51,6 +53,7 @@ struct TreeRoot {
   double inv;           // RN(1 / size)
   long long margin;     // 0: fast keys allowed; -1: the FP64 recurrence for every particle
   int bad;              // a particle position or mass is NaN or infinite
+  int lsb_m, lsb_f;     // fixed-point units (2^lsb) of the mass and first-moment sums
 };
 
 // ---------------------------------------------------------------------------
@@ -59,19 +62,23 @@ struct TreeRoot {
 constexpr int BB_THREADS = 256;
 constexpr int BB_BLOCKS = 304;
 
-// Per block: the box (min xyz, max xyz) and whether any position or mass is not
-// finite (the reference's insert never terminates on such particles), 7 doubles.
-constexpr int BB_PART = 7;
+// Per block: the box (min xyz, max xyz), whether any position or mass is not finite
+// (the reference's insert never terminates on such particles) and the largest |mass|,
+// 8 doubles.
+constexpr int BB_PART = 8;
 
 __global__ void __launch_bounds__(BB_THREADS)
     bbox_partial_kernel(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n,
                         double* __restrict__ part) {
   __shared__ double s_mn[3][BB_THREADS], s_mx[3][BB_THREADS];
-  double mn[3], mx[3];
+  __shared__ double s_m[BB_THREADS];
+  double mn[3], mx[3], mmax = 0.0;
   bool have = false, bad = false;
   for (int64_t i = (int64_t)blockIdx.x * BB_THREADS + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * BB_THREADS) {
-    bad = bad || !isfinite(mass[i]);
+    const double mi = mass[i];
+    bad = bad || !isfinite(mi);
+    mmax = fmax(mmax, fabs(mi));
 #pragma unroll
     for (int k = 0; k < 3; k++) {
       double q = pos[3 * i + k];
@@ -97,6 +104,7 @@ __global__ void __launch_bounds__(BB_THREADS)
     s_mn[k][threadIdx.x] = mn[k];
     s_mx[k][threadIdx.x] = mx[k];
   }
+  s_m[threadIdx.x] = mmax;
   bad = __syncthreads_or(bad);
   for (int s = BB_THREADS / 2; s > 0; s >>= 1) {
     if (threadIdx.x < s) {
@@ -106,6 +114,7 @@ __global__ void __launch_bounds__(BB_THREADS)
         if (a < s_mn[k][threadIdx.x]) s_mn[k][threadIdx.x] = a;
         if (b > s_mx[k][threadIdx.x]) s_mx[k][threadIdx.x] = b;
       }
+      s_m[threadIdx.x] = fmax(s_m[threadIdx.x], s_m[threadIdx.x + s]);
     }
     __syncthreads();
   }
@@ -116,6 +125,7 @@ __global__ void __launch_bounds__(BB_THREADS)
       part[BB_PART * blockIdx.x + 3 + k] = s_mx[k][0];
     }
     part[BB_PART * blockIdx.x + 6] = bad ? 1.0 : 0.0;
+    part[BB_PART * blockIdx.x + 7] = s_m[0];
   }
 }
 
@@ -137,7 +147,7 @@ __global__ void root_kernel(const double* __restrict__ part, int nb, double eps,
   if (blockIdx.x) return;
   const int lane = threadIdx.x;
   const double inf = __longlong_as_double(0x7ff0000000000000ll);
-  double mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf};
+  double mn[3] = {inf, inf, inf}, mx[3] = {-inf, -inf, -inf}, mmax = 0.0;
   bool bad = false;
   for (int b = lane; b < nb; b += 32) {
     for (int k = 0; k < 3; k++) {
@@ -146,8 +156,10 @@ __global__ void root_kernel(const double* __restrict__ part, int nb, double eps,
       if (c > mx[k]) mx[k] = c;
     }
     bad = bad || part[BB_PART * b + 6] != 0.0;
+    mmax = fmax(mmax, part[BB_PART * b + 7]);
   }
   bad = __any_sync(0xffffffffu, bad);
+  for (int o = 16; o > 0; o >>= 1) mmax = fmax(mmax, __shfl_xor_sync(0xffffffffu, mmax, o));
   for (int o = 16; o > 0; o >>= 1)
     for (int k = 0; k < 3; k++) {
       const double a = __shfl_xor_sync(0xffffffffu, mn[k], o), c = __shfl_xor_sync(0xffffffffu, mx[k], o);
@@ -165,6 +177,18 @@ __global__ void root_kernel(const double* __restrict__ part, int nb, double eps,
   }
   root->size = bs;
   root->bad = bad ? 1 : 0;
+  // fixed-point units: |m| < 2^Bm and |m x| < 2^(Bm + Bx + 1) (the product's rounding
+  // included), headroom for 2^24 particles (fixed192.cuh); floored so that sums of
+  // exotic tiny inputs stay normal doubles
+  if (!bad) {
+    double xmax = 0.0;
+    for (int k = 0; k < 3; k++) xmax = fmax(xmax, fmax(fabs(mn[k]), fabs(mx[k])));
+    const int bm = fx::bound_exponent(mmax), bx = fx::bound_exponent(xmax);
+    root->lsb_m = max(bm - fx::FX_HEADROOM, -1000);
+    root->lsb_f = max(bm + bx + 1 - fx::FX_HEADROOM, -1000);
+  } else {
+    root->lsb_m = root->lsb_f = 0;
+  }
   root->inv = ddiv(1.0, bs);
   root->margin = (bs > 0x1p-900 && bs < 0x1p+900 && amax < 0x1p+900) ? 0 : -1;
 }
@@ -397,12 +421,35 @@ struct NodeArrays {
   WalkRec* R;    // walk records (A, L, O)
   dvec4* C;      // (cx, cy, cz, size)                    exact opening test (internal cells)
   dvec4* M;      // (comx, comy, comz, mass)              interaction
-  dvec4* F;      // (first moment x, y, z, mass)          build only
-  int* parent;   // enclosing cell, -1 for the root        build only
-  int* nchild;   // number of child cells                  build only
-  int* kids;     // child cell per octant (8 per cell, -1 none)  build only
-  int* arrive;   // children whose monopole is done        build only
 };
+
+// Exact prefix sums over the key-ordered particles: mass and first moment x, y, z.
+struct FxMoments {
+  fx::I192 c[4];
+};
+constexpr int MS_THREADS = 256, MS_ITEMS = 8, MS_TILE = MS_THREADS * MS_ITEMS;
+
+__device__ __forceinline__ void fxm_add(FxMoments& a, const FxMoments& b) {
+#pragma unroll
+  for (int k = 0; k < 4; k++) a.c[k] = fx::add(a.c[k], b.c[k]);
+}
+
+__device__ __forceinline__ FxMoments fxm_zero() {
+  FxMoments r;
+#pragma unroll
+  for (int k = 0; k < 4; k++) r.c[k] = fx::zero();
+  return r;
+}
+
+// Prefix over the first j key-ordered particles (j <= n): the tile's prefix plus the
+// prefix within the tile.
+__device__ __forceinline__ FxMoments fxm_prefix(const FxMoments* __restrict__ local,
+                                                const FxMoments* __restrict__ tiles, int64_t j, int64_t n) {
+  if (j >= n) return tiles[(n + MS_TILE - 1) / MS_TILE];
+  FxMoments r = tiles[j / MS_TILE];
+  fxm_add(r, local[j]);
+  return r;
+}
 
 __device__ __forceinline__ float f32_hi(double v) { return (float)v; }
 __device__ __forceinline__ float f32_lo(double v, float hi) { return (float)(v - (double)hi); }
@@ -433,76 +480,48 @@ __device__ __forceinline__ int64_t cell_end(const uint64_t* __restrict__ keys, i
   return a + 1;
 }
 
-// First particle of the level-L cell that holds particle i (L <= lp[i]).
-__device__ __forceinline__ int64_t cell_begin(const uint64_t* __restrict__ keys, int words, int64_t n,
-                                              const int* __restrict__ lp, int64_t i, int L) {
-  int64_t j = i;
-  for (int s = 0; s < 16; s++, j--)
-    if (lp[j] < L) return j;  // lp[0] = -1 ends the scan
-  int64_t a = 0, b = j;  // b shares >= L digits with i
-  for (int64_t step = 32; b - step > a; step *= 2) {
-    if (key_lcp(keys, words, n, b - step, i) < L) {
-      a = b - step + 1;
-      break;
-    }
-    b -= step;
-  }
-  while (a < b) {
-    const int64_t mid = (a + b) >> 1;
-    if (key_lcp(keys, words, n, mid, i) >= L)
-      b = mid;
-    else
-      a = mid + 1;
-  }
-  return a;
-}
-
 // Particle i opens the cells at levels lo = lp[i]+1 .. d (its leaf), nodes
-// base[i] .. base[i] + d - lo in preorder.  nodes_kernel records each cell's
-// enclosing cell (counting itself there) and the leaf's skip index, and lists the
+// base[i] .. base[i] + d - lo in preorder.  nodes_kernel writes the leaf: the
+// particle's position as its centre, its mass, its skip index (gravoct_finalize,
+// _jbgrav.c:467-483: a leaf's centre of mass is its particle), and lists the
 // particles that open internal cells; nodes_internal_kernel gives those cells their
 // centre from the reference's FP64 recurrence along the particle's digits
-// (gravoct_add_particle, _jbgrav.c:403-428) and their skip index.  A leaf is always
-// accepted by the walk, so it needs no centre.
-__global__ void nodes_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
-                             const int* __restrict__ lp, const int* __restrict__ depth,
-                             const int* __restrict__ base, NodeArrays na, int nnodes, int* __restrict__ list,
-                             int* __restrict__ count) {
+// (gravoct_add_particle, _jbgrav.c:403-428), their skip index and their monopole.  A
+// leaf is always accepted by the walk, so it needs no geometric centre.
+__global__ void nodes_kernel(int64_t n, const int* __restrict__ lp, const int* __restrict__ depth,
+                             const int* __restrict__ base, const uint32_t* __restrict__ perm,
+                             const double* __restrict__ pos, const double* __restrict__ mass, NodeArrays na,
+                             int nnodes, int* __restrict__ list, int* __restrict__ count) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
   if (i < n) {
     const int lo = lp[i] + 1, d = depth[i];
-    const int k0 = base[i];
-    int par = -1;
-    if (lo > 0) {
-      const int64_t j0 = cell_begin(keys, words, n, lp, i, lo - 1);
-      par = base[j0] + (lo - 1) - (lp[j0] + 1);
-    }
-    for (int L = lo; L <= d; L++) {
-      const int k = k0 + (L - lo);
-      const int pk = L == lo ? par : k - 1;
-      na.parent[k] = pk;
-      if (pk >= 0) {
-        atomicAdd(&na.nchild[pk], 1);
-        na.kids[8 * pk + key_digit(keys, n, i, L - 1)] = k;
-      }
-    }
-    const int k = k0 + (d - lo);
+    const int k = base[i] + (d - lo);
     const int next = i + 1 < n ? base[i + 1] : nnodes;
-    na.R[k].A = make_float4(0.f, 0.f, 0.f, 0.f);
-    na.R[k].L = make_float4(0.f, 0.f, 0.f, __int_as_float(next));
+    const int64_t p = perm[i];
+    const double m = mass[p];
+    const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
+    na.M[k] = make_dvec4(x, y, z, m);
+    const float hx = (float)x, hy = (float)y, hz = (float)z;
+    na.R[k].A = make_float4(hx, hy, hz, 0.f);
+    na.R[k].L = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), __int_as_float(next));
+    na.R[k].O = make_float4(0.f, 0.f, 0.f, (float)m);
     need = d > lo;
   }
   warp_append(need, i, list, count);
 }
 
+__device__ __forceinline__ double rcp_f64(double m);
+
 __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
                                       const int* __restrict__ lp, const int* __restrict__ depth,
                                       const int* __restrict__ base, const TreeRoot* __restrict__ root,
                                       NodeArrays na, int nnodes, const int* __restrict__ list,
-                                      const int* __restrict__ count) {
+                                      const int* __restrict__ count, const FxMoments* __restrict__ fx_local,
+                                      const FxMoments* __restrict__ fx_tiles) {
   __shared__ double offs[TREE_MAX_LEVELS];  // size 2^-(L+2), exact
   const double S = root->size;
+  const int lsb_m = root->lsb_m, lsb_f = root->lsb_f;
   for (int l = threadIdx.x; l < TREE_MAX_LEVELS; l += blockDim.x)
     offs[l] = dmul(S, __longlong_as_double((long long)(1023 - (l + 2)) << 52));
   __syncthreads();
@@ -511,6 +530,7 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
     const int64_t i = list[q];
     const int lo = lp[i] + 1, d = depth[i];
     const int k0 = base[i];
+    const FxMoments Pi = fxm_prefix(fx_local, fx_tiles, i, n);  // every cell i opens starts at i
     const uint64_t kw0 = keys[i], kw1 = words > 1 ? keys[n + i] : 0ull;  // digits of the first 42 levels
     double c[3] = {root->c[0], root->c[1], root->c[2]};
     for (int L = 0; L < d; L++) {
@@ -531,6 +551,17 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
         na.R[k].A = A;
         na.R[k].L = Lo;
         na.C[k] = make_dvec4(c[0], c[1], c[2], size);
+        // monopole of particles [i, end): exact sums, one rounding each, then
+        // firstmoment / mass (_jbgrav.c:478) with a Newton-refined reciprocal
+        const FxMoments Pe = fxm_prefix(fx_local, fx_tiles, end, n);
+        const double cm = fx::to_double(fx::sub(Pe.c[0], Pi.c[0]), lsb_m);
+        const double r = rcp_f64(cm);
+        double com[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) com[a] = dmul(fx::to_double(fx::sub(Pe.c[a + 1], Pi.c[a + 1]), lsb_f), r);
+        na.M[k] = make_dvec4(com[0], com[1], com[2], cm);
+        na.R[k].O = make_float4((float)dsub(com[0], c[0]), (float)dsub(com[1], c[1]), (float)dsub(com[2], c[2]),
+                                (float)cm);
       }
       if (L + 1 < d) {
         const unsigned g = L < KEY_LEVELS       ? (unsigned)(kw0 >> (3 * (KEY_LEVELS - 1 - L))) & 7u
@@ -545,20 +576,13 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
 }
 
 // ---------------------------------------------------------------------------
-// 5. Monopole pass, bottom-up in one launch
+// 5. Exact prefix sums of the monopole moments over the key-ordered particles
 // ---------------------------------------------------------------------------
-// Each particle sets its leaf (gravoct_finalize, _jbgrav.c:467-483: the particle's own
-// position and mass) and climbs: the child that arrives last at a cell (per-cell
-// counter) sums the cell's children in preorder and climbs on.  The sums do not
-// depend on which child arrives last, so the result is deterministic.
-__device__ __forceinline__ int node_next(const WalkRec* __restrict__ R, int k) { return __float_as_int(R[k].L.w); }
-
-
-__device__ __forceinline__ int atomic_add_acq_rel(int* p, int v) {
-  int old;
-  asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], %2;" : "=r"(old) : "l"(p), "r"(v) : "memory");
-  return old;
-}
+// The particles of a cell are a contiguous range [first, end) of the key order, so
+// its mass and first moment (m_j x_j, the reference's FP64 products,
+// gravoct_add_particle, _jbgrav.c:396-398) are differences of prefix sums.  The sums
+// are exact 192-bit fixed-point integers (fixed192.cuh): their values do not depend on
+// the order of addition, and each cell's is rounded to FP64 once.
 
 // 1/m from the hardware approximation and two Newton steps y <- y + y (1 - m y).
 __device__ __forceinline__ double rcp_f64(double m) {
@@ -569,70 +593,76 @@ __device__ __forceinline__ double rcp_f64(double m) {
   return y;
 }
 
-__global__ void com_up_kernel(NodeArrays na, int64_t n, const int* __restrict__ lp, const int* __restrict__ depth,
-                              const int* __restrict__ base, const uint32_t* __restrict__ perm,
-                              const double* __restrict__ pos, const double* __restrict__ mass) {
-  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  int cur = base[i] + (depth[i] - (lp[i] + 1));
-  {
-    const int64_t p = perm[i];
-    const double m = mass[p];
-    const double x = pos[3 * p], y = pos[3 * p + 1], z = pos[3 * p + 2];
-    na.M[cur] = make_dvec4(x, y, z, m);
-    na.F[cur] = make_dvec4(dmul(m, x), dmul(m, y), dmul(m, z), m);
-    // walk record: the particle's position as the leaf's centre (hi/lo), zero offset
-    const float hx = (float)x, hy = (float)y, hz = (float)z;
-    na.R[cur].A = make_float4(hx, hy, hz, 0.f);
-    na.R[cur].L = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), na.R[cur].L.w);
-    na.R[cur].O = make_float4(0.f, 0.f, 0.f, (float)m);
-  }
-  for (;;) {
-    const int par = na.parent[cur];
-    if (par < 0) break;
-    // release this child's moments, acquire the siblings' (one acq_rel RMW on the counter)
-    if (atomic_add_acq_rel(&na.arrive[par], 1) != na.nchild[par] - 1) break;
-    // children in preorder = in octant order; their slots are known, so the loads of
-    // their moments are independent
-    const int4 ka = reinterpret_cast<const int4*>(na.kids)[2 * par];
-    const int4 kb = reinterpret_cast<const int4*>(na.kids)[2 * par + 1];
-    const int kid[8] = {ka.x, ka.y, ka.z, ka.w, kb.x, kb.y, kb.z, kb.w};
-    double fx = 0.0, fy = 0.0, fz = 0.0, m = 0.0;
+__device__ __forceinline__ FxMoments particle_moments(const double* __restrict__ pos,
+                                                      const double* __restrict__ mass, int64_t p, int lsb_m,
+                                                      int lsb_f) {
+  const double m = mass[p];
+  FxMoments r;
+  r.c[0] = fx::from_double(m, lsb_m);
 #pragma unroll
-    for (int o = 0; o < 8; o++) {
-      if (kid[o] < 0) continue;
-      const double2* f = reinterpret_cast<const double2*>(na.F + kid[o]);
-      const double2 fa = __ldcg(f), fb = __ldcg(f + 1);  // siblings were written by other threads
-      fx = dadd(fx, fa.x);
-      fy = dadd(fy, fa.y);
-      fz = dadd(fz, fb.x);
-      m = dadd(m, fb.y);
-    }
-    na.F[par] = make_dvec4(fx, fy, fz, m);
-    cur = par;
-  }
+  for (int a = 0; a < 3; a++) r.c[a + 1] = fx::from_double(dmul(m, pos[3 * p + a]), lsb_f);
+  return r;
 }
 
-// Centres of mass of the internal cells, on full warps (the climb above runs on few
-// lanes per warp, and GB300 issues FP64 at 1/74 of the FP32 rate): firstmoment / mass
-// (_jbgrav.c:478) as a product with a Newton-refined reciprocal, within an ulp or two of
-// the quotient.  The listed particles are the ones that opened internal cells.
-__global__ void com_final_kernel(NodeArrays na, const int* __restrict__ lp, const int* __restrict__ depth,
-                                 const int* __restrict__ base, const int* __restrict__ list,
-                                 const int* __restrict__ count) {
-  const int cnt = *count;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < cnt; q += gridDim.x * blockDim.x) {
-    const int64_t i = list[q];
-    const int k0 = base[i], internal = depth[i] - (lp[i] + 1);  // cells k0 .. k0+internal-1
-    for (int k = k0; k < k0 + internal; k++) {
-      const dvec4 F = na.F[k];
-      const double r = rcp_f64(F.w);
-      const double cx = dmul(F.x, r), cy = dmul(F.y, r), cz = dmul(F.z, r);
-      na.M[k] = make_dvec4(cx, cy, cz, F.w);
-      const dvec4 C = na.C[k];
-      na.R[k].O = make_float4((float)dsub(cx, C.x), (float)dsub(cy, C.y), (float)dsub(cz, C.z), (float)F.w);
-    }
+// Exclusive scan of the threads' totals within a block of MS_THREADS; returns the
+// thread's exclusive prefix.
+__device__ __forceinline__ FxMoments fxm_block_exclusive(const FxMoments& tot) {
+  __shared__ FxMoments warp_tot[MS_THREADS / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  FxMoments inc = tot;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    FxMoments y;
+#pragma unroll
+    for (int k = 0; k < 4; k++)
+#pragma unroll
+      for (int w = 0; w < 3; w++) y.c[k].w[w] = __shfl_up_sync(0xffffffffu, inc.c[k].w[w], d);
+    if (lane >= d) fxm_add(inc, y);
   }
+  if (lane == 31) warp_tot[warp] = inc;
+  __syncthreads();
+  FxMoments before = fxm_zero();
+  for (int w = 0; w < warp; w++) fxm_add(before, warp_tot[w]);
+#pragma unroll
+  for (int k = 0; k < 4; k++) before.c[k] = fx::add(before.c[k], fx::sub(inc.c[k], tot.c[k]));
+  __syncthreads();  // warp_tot may be reused by the caller's next scan
+  return before;
+}
+
+// Per tile of MS_TILE key-ordered particles: the prefix of every particle within its
+// tile (fx_local) and the tile's total (fx_tiles[tile]).
+__global__ void __launch_bounds__(MS_THREADS)
+    moments_scan_kernel(const double* __restrict__ pos, const double* __restrict__ mass,
+                        const uint32_t* __restrict__ perm, int64_t n, const TreeRoot* __restrict__ root,
+                        FxMoments* __restrict__ fx_local, FxMoments* __restrict__ fx_tiles) {
+  const int lsb_m = root->lsb_m, lsb_f = root->lsb_f;
+  const int64_t j0 = (int64_t)blockIdx.x * MS_TILE + (int64_t)threadIdx.x * MS_ITEMS;
+  FxMoments tot = fxm_zero();
+  for (int r = 0; r < MS_ITEMS; r++)
+    if (j0 + r < n) fxm_add(tot, particle_moments(pos, mass, perm[j0 + r], lsb_m, lsb_f));
+  FxMoments run = fxm_block_exclusive(tot);
+  for (int r = 0; r < MS_ITEMS; r++)
+    if (j0 + r < n) {
+      fx_local[j0 + r] = run;
+      fxm_add(run, particle_moments(pos, mass, perm[j0 + r], lsb_m, lsb_f));
+    }
+  if (threadIdx.x == MS_THREADS - 1) fx_tiles[blockIdx.x] = run;
+}
+
+// Exclusive scan of the tile totals in place; fx_tiles[ntiles] receives the total.
+__global__ void __launch_bounds__(MS_THREADS) moments_tiles_kernel(FxMoments* __restrict__ fx_tiles, int64_t ntiles) {
+  const int64_t per = (ntiles + MS_THREADS - 1) / MS_THREADS;
+  const int64_t a = (int64_t)threadIdx.x * per;
+  const int64_t b = a + per < ntiles ? a + per : ntiles;
+  FxMoments tot = fxm_zero();
+  for (int64_t t = a; t < b; t++) fxm_add(tot, fx_tiles[t]);
+  FxMoments run = fxm_block_exclusive(tot);
+  for (int64_t t = a; t < b; t++) {
+    const FxMoments v = fx_tiles[t];
+    fx_tiles[t] = run;
+    fxm_add(run, v);
+  }
+  if (threadIdx.x == MS_THREADS - 1) fx_tiles[ntiles] = run;
 }
 
 // ---------------------------------------------------------------------------
@@ -809,7 +839,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
 // ---------------------------------------------------------------------------
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
-  Buffer nA, nC, nM, nF, parent, nchild, arrive, kids, xh[2];
+  Buffer nA, nC, nM, fxl, fxt, xh[2];
   Buffer list;                // particle lists: key fallbacks, then cell openers
   int* host_flags = nullptr;  // pinned: the 8 device flags, nnodes, the root's non-finite flag
   int words = TREE_MIN_WORDS;
@@ -823,11 +853,6 @@ static NodeArrays node_arrays(TreeWS& ws) {
   na.R = (WalkRec*)ws.nA.ptr;
   na.C = (dvec4*)ws.nC.ptr;
   na.M = (dvec4*)ws.nM.ptr;
-  na.F = (dvec4*)ws.nF.ptr;
-  na.parent = (int*)ws.parent.ptr;
-  na.nchild = (int*)ws.nchild.ptr;
-  na.kids = (int*)ws.kids.ptr;
-  na.arrive = (int*)ws.arrive.ptr;
   return na;
 }
 
@@ -936,35 +961,31 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.nA, (size_t)nnodes * sizeof(WalkRec)));
   GH_TRY(ensure(ws.nC, (size_t)nnodes * sizeof(dvec4)));
   GH_TRY(ensure(ws.nM, (size_t)nnodes * sizeof(dvec4)));
-  GH_TRY(ensure(ws.nF, (size_t)nnodes * sizeof(dvec4)));
-  GH_TRY(ensure(ws.parent, (size_t)nnodes * sizeof(int)));
-  GH_TRY(ensure(ws.nchild, (size_t)nnodes * sizeof(int)));
-  GH_TRY(ensure(ws.arrive, (size_t)nnodes * sizeof(int)));
-  GH_TRY(ensure(ws.kids, (size_t)nnodes * 8 * sizeof(int)));
+  const int64_t ntiles = (n + MS_TILE - 1) / MS_TILE;
+  GH_TRY(ensure(ws.fxl, (size_t)n * sizeof(FxMoments)));
+  GH_TRY(ensure(ws.fxt, (size_t)(ntiles + 1) * sizeof(FxMoments)));
   NodeArrays na = node_arrays(ws);
-  GH_CUDA_TRY(cudaMemsetAsync(ws.nchild.ptr, 0, (size_t)nnodes * sizeof(int), st));
-  GH_CUDA_TRY(cudaMemsetAsync(ws.arrive.ptr, 0, (size_t)nnodes * sizeof(int), st));
-  GH_CUDA_TRY(cudaMemsetAsync(ws.kids.ptr, 0xff, (size_t)nnodes * 8 * sizeof(int), st));
   {
     const uint64_t* keys = (const uint64_t*)ws.keys.ptr;
     const int* lp = (const int*)ws.lp.ptr;
     const int* dep = (const int*)ws.depth.ptr;
     const int* bs = (const int*)ws.base.ptr;
+    const uint32_t* perm = (const uint32_t*)ws.idx.ptr;
     int* openers = (int*)ws.flags.ptr + 4;
-    nodes_kernel<<<gn, T, 0, st>>>(keys, words, n, lp, dep, bs, na, nnodes, (int*)ws.list.ptr, openers);
+    FxMoments* fxl = (FxMoments*)ws.fxl.ptr;
+    FxMoments* fxt = (FxMoments*)ws.fxt.ptr;
+    // 5. exact prefix sums of the moments (the cells' monopoles come from them below)
+    moments_scan_kernel<<<(unsigned)ntiles, MS_THREADS, 0, st>>>(pos, mass, perm, n, root, fxl, fxt);
+    GH_LAUNCH_CHECK();
+    moments_tiles_kernel<<<1, MS_THREADS, 0, st>>>(fxt, ntiles);
+    GH_LAUNCH_CHECK();
+    // 4. leaves, then internal cells with their centres and monopoles
+    nodes_kernel<<<gn, T, 0, st>>>(n, lp, dep, bs, perm, pos, mass, na, nnodes, (int*)ws.list.ptr, openers);
     GH_LAUNCH_CHECK();
     nodes_internal_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(keys, words, n, lp, dep, bs, root, na, nnodes,
-                                                                    (const int*)ws.list.ptr, openers);
+                                                                    (const int*)ws.list.ptr, openers, fxl, fxt);
     GH_LAUNCH_CHECK();
   }
-  // 5. monopoles
-  com_up_kernel<<<gn, T, 0, st>>>(na, n, (const int*)ws.lp.ptr, (const int*)ws.depth.ptr, (const int*)ws.base.ptr,
-                                  (const uint32_t*)ws.idx.ptr, pos, mass);
-  GH_LAUNCH_CHECK();
-  com_final_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(na, (const int*)ws.lp.ptr, (const int*)ws.depth.ptr,
-                                                              (const int*)ws.base.ptr, (const int*)ws.list.ptr,
-                                                              (const int*)ws.flags.ptr + 4);
-  GH_LAUNCH_CHECK();
   out->nnodes = nnodes;
   out->maxdepth = maxdepth;
   return GH_OK;
