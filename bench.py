@@ -486,6 +486,7 @@ def measure_tree(dev, n=1 << 20, steps=2):
                               "exact_tests_per_target": c["exact_tests"] / n,
                               "leaf_interactions_per_target": c["leaf_interactions"] / n,
                               "warp_cell_steps": c["cell_steps"],
+                              "single_child_step_frac": c["chain_steps"] / max(c["cell_steps"], 1),
                               "record_bytes_per_walk": rec_bytes,
                               "record_read_gbs": rec_bytes / walk_s / 1e9,
                               "record_read_frac_of_measured_l2": rec_bytes / walk_s / l2,

@@ -196,11 +196,11 @@ def tree_stats(enable: bool) -> None:
 def tree_stats_read():
     """Counters since the last read: walks, warp cell steps (48-byte records read),
     cells visited summed over targets, target-cell interactions, exact FP64 opening
-    tests, interactions with leaves."""
-    out = (ctypes.c_int64 * 6)()
+    tests, interactions with leaves, warp steps at single-child cells."""
+    out = (ctypes.c_int64 * 7)()
     call("gh_tree_stats_read", ctypes.addressof(out))
     return {"walks": out[0], "cell_steps": out[1], "target_visits": out[2], "interactions": out[3],
-            "exact_tests": out[4], "leaf_interactions": out[5]}
+            "exact_tests": out[4], "leaf_interactions": out[5], "chain_steps": out[6]}
 
 
 def inject(fault: int, count: int = 1) -> None:

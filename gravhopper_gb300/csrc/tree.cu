@@ -717,11 +717,16 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
   float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
   float hx = 0.f, hy = 0.f, hz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;  // two-sum hi, lo
   int pending = 0;
-  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0, n_leaf = 0;  // walk counters (STATS)
+  unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0, n_leaf = 0, n_chain = 0;  // walk counters (STATS)
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
   while (node < nnodes) {
-    if (STATS) n_step++;
+    if (STATS) {
+      n_step++;
+      // a cell with one child cell: the child's subtree ends where the cell's does
+      const int nxt = __float_as_int(nR[node].L.w);
+      if (nxt != node + 1 && node + 1 < nnodes && __float_as_int(nR[node + 1].L.w) == nxt) n_chain++;
+    }
     int lane_next = skip;
     if (node >= skip) {
       if (STATS) n_visit++;
@@ -824,6 +829,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       atomicAdd(&stats[2], (unsigned long long)n_inter);
       atomicAdd(&stats[3], (unsigned long long)n_exact);
       atomicAdd(&stats[4], (unsigned long long)n_leaf);
+      atomicAdd(&stats[5], (unsigned long long)n_chain);
     }
   }
   if (MIXED) {
@@ -1138,7 +1144,7 @@ extern "C" int gh_tree_stats_read(int64_t* out) {
   DeviceInfo di;
   GH_TRY(device_info(&di));
   Buffer& b = g_stats[di.device];
-  unsigned long long h[5] = {0, 0, 0, 0, 0};
+  unsigned long long h[6] = {0, 0, 0, 0, 0, 0};
   if (b.ptr) {
     GH_CUDA_TRY(cudaDeviceSynchronize());
     GH_CUDA_TRY(cudaMemcpy(h, b.ptr, sizeof(h), cudaMemcpyDeviceToHost));
@@ -1146,7 +1152,7 @@ extern "C" int gh_tree_stats_read(int64_t* out) {
     GH_CUDA_TRY(cudaDeviceSynchronize());
   }
   out[0] = g_stats_walks;
-  for (int k = 0; k < 5; k++) out[k + 1] = (int64_t)h[k];
+  for (int k = 0; k < 6; k++) out[k + 1] = (int64_t)h[k];
   g_stats_walks = 0;
   return GH_OK;
 }

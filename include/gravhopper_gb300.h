@@ -227,9 +227,10 @@ int gh_check_inv_cube(int64_t n, uint64_t seed, long long* wrong_fallback, void*
 int gh_tree_stats(int enable);
 
 /* Synchronises the device and returns the counters accumulated since the last read,
- * then clears them (out holds 6 entries): out[0] walks, out[1] warp cell steps,
+ * then clears them (out holds 7 entries): out[0] walks, out[1] warp cell steps,
  * out[2] target cell visits, out[3] interactions, out[4] exact opening tests,
- * out[5] interactions with leaves. */
+ * out[5] interactions with leaves, out[6] warp steps at cells with a single child
+ * cell (the uncompressed octree's chains). */
 int gh_tree_stats_read(int64_t* out);
 
 /* ---- fault injection for tests (no counterpart in the reference) ----------------- */
