@@ -15,8 +15,8 @@
 //      words ordered by the other words (a full multi-word radix sort for long runs);
 //   4. the node set of the reference's uncompressed octree (every cell that holds a
 //      particle and whose parent holds at least two, single-child chains included)
-//      laid out in depth-first preorder with skip ("next") indices and parent links,
-//      from the common prefix lengths of neighbouring keys;
+//      laid out in depth-first preorder with skip ("next") indices, from the common
+//      prefix lengths of neighbouring keys;
 //   5. monopoles: leaves take the particle's position and mass exactly
 //      (gravoct_finalize, _jbgrav.c:467-483); a cell holds a contiguous range of the
 //      key-ordered particles, so its mass and first moment are differences of exact
@@ -637,6 +637,9 @@ __global__ void __launch_bounds__(MS_THREADS)
                         FxMoments* __restrict__ fx_local, FxMoments* __restrict__ fx_tiles) {
   const int lsb_m = root->lsb_m, lsb_f = root->lsb_f;
   const int64_t j0 = (int64_t)blockIdx.x * MS_TILE + (int64_t)threadIdx.x * MS_ITEMS;
+  // each item's moments are formed twice (for the thread's total, then for the running
+  // prefix): measured cheaper than storing them and reading them back (1.22 against
+  // 1.33 ms per build at N = 1M)
   FxMoments tot = fxm_zero();
   for (int r = 0; r < MS_ITEMS; r++)
     if (j0 + r < n) fxm_add(tot, particle_moments(pos, mass, perm[j0 + r], lsb_m, lsb_f));
