@@ -292,6 +292,25 @@ __global__ void keys_exact_kernel(const double* __restrict__ pos, int64_t n, con
   }
 }
 
+// Keys of target points (two words, 42 levels of the sources' root cell; points
+// outside it clamped to its faces) for the walk's order only: warps that hold
+// neighbouring targets visit nearly the same cells.  Any order gives each target the
+// same decisions and interactions, so these keys need not be the reference's.
+__global__ void target_keys_kernel(const double* __restrict__ tpos, int64_t nt, const TreeRoot* __restrict__ root,
+                                   uint64_t* __restrict__ keys, uint32_t* __restrict__ idx) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nt) return;
+  uint64_t T[3];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    const double t = fma(tpos[3 * i + k] - root->c[k], root->inv, 0.5);
+    T[k] = t >= 1.0 ? ((1ull << 63) - 1) : (t > 0.0 ? (uint64_t)(t * 0x1p63) : 0ull);  // NaN: 0
+  }
+  keys[i] = spread3(T[0] >> 42) | (spread3(T[1] >> 42) << 1) | (spread3(T[2] >> 42) << 2);
+  keys[nt + i] = spread3(T[0] >> 21) | (spread3(T[1] >> 21) << 1) | (spread3(T[2] >> 21) << 2);
+  idx[i] = (uint32_t)i;
+}
+
 __device__ __forceinline__ int key_lcp(const uint64_t* __restrict__ keys, int words, int64_t n, int64_t a,
                                        int64_t b) {
   for (int w = 0; w < words; w++) {
@@ -849,6 +868,7 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
 struct TreeWS {
   Buffer part, root, keys, keys_tmp, idx, idx_tmp, rs, lp, cnt, depth, base, scan, flags;
   Buffer nA, nC, nM, fxl, fxt, xh[2];
+  Buffer tkeys, tkeys_tmp, tidx, tidx_tmp, trs;  // target points' walk order
   Buffer list;                // particle lists: key fallbacks, then cell openers
   int* host_flags = nullptr;  // pinned: the 8 device flags, nnodes, the root's non-finite flag
   int words = TREE_MIN_WORDS;
@@ -868,10 +888,18 @@ static NodeArrays node_arrays(TreeWS& ws) {
 struct BuiltTree {
   int nnodes = 0;
   int maxdepth = 0;
+  const uint32_t* torder = nullptr;  // target points in key order (when sorted)
 };
 
+// Target points are walked in key order from this many on (below, the sort's fixed
+// cost exceeds what the coherent warps save).
+constexpr int64_t TGT_SORT_MIN = 8192;
+
 static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t n, double eps,
-                      cudaStream_t st, BuiltTree* out) {
+                      cudaStream_t st, BuiltTree* out, const double* tpos = nullptr, int64_t nt = 0) {
+  const bool sort_targets = tpos != nullptr && nt >= TGT_SORT_MIN;
+  if (sort_targets && nt > (1LL << 31))
+    return set_error(GH_ERR_ARG, "tree: at most 2^31 target points (got %lld)", (long long)nt);
   // int32 node indices: at most 127 cells per particle
   if (n > (1LL << 24)) return set_error(GH_ERR_ARG, "tree: at most 16777216 particles (got %lld)", (long long)n);
   if (!ws.host_flags) GH_CUDA_TRY(cudaMallocHost((void**)&ws.host_flags, 16 * sizeof(int)));
@@ -939,6 +967,19 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
                                    (int*)ws.flags.ptr);
     GH_LAUNCH_CHECK();
     GH_TRY(exclusive_scan_i32((const int*)ws.cnt.ptr, (int*)ws.base.ptr, n, (int*)ws.scan.ptr, st));
+    if (sort_targets) {  // the targets' walk order; its sort reports a given-up wait in flags[5] too
+      GH_TRY(ensure(ws.tkeys, (size_t)2 * nt * sizeof(uint64_t)));
+      GH_TRY(ensure(ws.tkeys_tmp, (size_t)2 * nt * sizeof(uint64_t)));
+      GH_TRY(ensure(ws.tidx, (size_t)nt * sizeof(uint32_t)));
+      GH_TRY(ensure(ws.tidx_tmp, (size_t)nt * sizeof(uint32_t)));
+      GH_TRY(ensure(ws.trs, radix_scratch_words(nt) * sizeof(uint32_t)));
+      target_keys_kernel<<<(unsigned)((nt + T - 1) / T), T, 0, st>>>(tpos, nt, root, (uint64_t*)ws.tkeys.ptr,
+                                                                     (uint32_t*)ws.tidx.ptr);
+      GH_LAUNCH_CHECK();
+      GH_TRY(radix_sort_keys((uint64_t*)ws.tkeys.ptr, (uint32_t*)ws.tidx.ptr, (uint64_t*)ws.tkeys_tmp.ptr,
+                             (uint32_t*)ws.tidx_tmp.ptr, 2, KEY_BITS, nt, (uint32_t*)ws.trs.ptr, st, flags + 5));
+      out->torder = (const uint32_t*)ws.tidx.ptr;
+    }
     GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags, ws.flags.ptr, 8 * sizeof(int), cudaMemcpyDeviceToHost, st));
     GH_CUDA_TRY(cudaMemcpyAsync(ws.host_flags + 8, (int*)ws.base.ptr + n, sizeof(int), cudaMemcpyDeviceToHost,
                                 st));
@@ -1089,10 +1130,10 @@ int tree_force(const double* pos, const double* mass, int64_t np, const double* 
   GH_TRY(device_info(&di));
   TreeWS& ws = g_tree[di.device];
   BuiltTree bt;
-  GH_TRY(tree_build(ws, pos, mass, np, eps, st, &bt));
+  GH_TRY(tree_build(ws, pos, mass, np, eps, st, &bt, self ? nullptr : tpos, self ? 0 : nt));
   EpiStore epi{acc};
   if (self) return tree_walk(ws, bt, pos, (const uint32_t*)ws.idx.ptr, np, eps, theta, precision, epi, st);
-  return tree_walk(ws, bt, tpos, nullptr, nt, eps, theta, precision, epi, st);
+  return tree_walk(ws, bt, tpos, bt.torder, nt, eps, theta, precision, epi, st);
 }
 
 int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nsteps, double dt, double eps,
