@@ -242,14 +242,16 @@ def test_tree_walk_counters(lib, cuda):
     assert _capi.tree_stats_read()["walks"] == 0
 
 
+@pytest.mark.parametrize("eps", [0.1, 0.0])
 @pytest.mark.parametrize("precision,rms_tol,max_tol", [("fp64", TREE_RMS_TOL, TREE_MAX_TOL),
                                                         ("mixed", MIXED_TREE_RMS_TOL, MIXED_TREE_MAX_TOL)])
-def test_tree_many_target_points_any_order(lib, cuda, precision, rms_tol, max_tol):
+def test_tree_many_target_points_any_order(lib, cuda, precision, rms_tol, max_tol, eps):
     """From 8192 target points on, the walk takes the targets in octant-key order (a
     radix sort of their keys in the sources' root cell; points outside it clamped to
     its faces) and writes each force to the target's own slot.  20,000 targets in
     random order, some outside the sources' box and some on particles, against the
-    reference tree's target-point form (gravhopper/_jbgrav.c:634-727)."""
+    reference tree's target-point form (gravhopper/_jbgrav.c:634-727), with softening
+    and with eps = 0 (a point on a particle gets no term from it)."""
     import torch
 
     from gravhopper_gb300 import engine, ics
@@ -260,6 +262,7 @@ def test_tree_many_target_points_any_order(lib, cuda, precision, rms_tol, max_to
     fp = fp[rng.permutation(len(fp))]
     x = torch.from_numpy(ic["pos"]).to(cuda)
     m = torch.from_numpy(ic["mass"]).to(cuda)
-    got = engine.tree_force(x, m, 0.1, 0.7, force_pos=torch.from_numpy(fp).to(cuda),
+    got = engine.tree_force(x, m, eps, 0.7, force_pos=torch.from_numpy(fp).to(cuda),
                             precision=precision).cpu().numpy()
-    check(got, oracle.tree_force_position(ic["pos"], ic["mass"], fp, 0.1, 0.7), rms_tol, max_tol)
+    assert np.isfinite(got).all()
+    check(got, oracle.tree_force_position(ic["pos"], ic["mass"], fp, eps, 0.7), rms_tol, max_tol)
