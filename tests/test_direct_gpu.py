@@ -194,3 +194,37 @@ def test_every_mixed_shape(lib, cuda):
             assert rms <= 1e-6 and mx <= 1e-3, (shape, rms, mx)
     finally:
         _capi.call("gh_direct_set_shape", -1)
+
+
+def test_inputs_cast_like_the_reference(lib, cuda):
+    """The reference casts any array-like to C-contiguous float64 before computing
+    (PyArray_FROM_OTF(obj, NPY_DOUBLE, NPY_ARRAY_IN_ARRAY), gravhopper/_jbgrav.c:79-86)
+    and reads masses through their first index only (:103): float32, Fortran-ordered,
+    strided and list inputs, integer and (N, 1) masses give the results of the same
+    values as C-contiguous float64 (bit for bit in the FP64 direct sum, within the tree
+    tolerance for the tree)."""
+    from gravhopper_gb300 import _jbgrav, ics
+    ic = ics.plummer(2400, seed=33)
+    base = ic["pos"]
+    rng = np.random.default_rng(4)
+    imass = rng.integers(1, 5, size=1200)
+    cases = [
+        (base[:1200].astype(np.float32), ic["mass"][:1200]),
+        (np.asfortranarray(base[:1200]), ic["mass"][:1200]),
+        (base[::2], ic["mass"][::2]),
+        (base[:1200].tolist(), list(ic["mass"][:1200])),
+        (base[:1200], imass),
+        (base[:1200], ic["mass"][:1200].reshape(-1, 1)),
+    ]
+    fp = rng.normal(size=(300, 3)).astype(np.float32) * 1e-3
+    for pos, mass in cases:
+        p64 = np.ascontiguousarray(pos, dtype=np.float64)
+        m64 = np.ascontiguousarray(mass, dtype=np.float64).reshape(len(p64), -1)[:, 0].copy()
+        np.testing.assert_array_equal(_jbgrav.direct_summation(pos, mass, 5e-5),
+                                      oracle.direct_summation(p64, m64, 5e-5))
+        np.testing.assert_array_equal(_jbgrav.direct_summation_position(pos, mass, fp, 5e-5),
+                                      oracle.direct_summation_position(p64, m64, fp.astype(np.float64), 5e-5))
+        got = _jbgrav.tree_force(pos, mass, 5e-5, 0.7)
+        ref = oracle.tree_force(p64, m64, 5e-5, 0.7)
+        r = np.linalg.norm(got - ref, axis=1) / np.linalg.norm(ref, axis=1)
+        assert np.sqrt(np.mean(r * r)) <= 1e-12 and r.max() <= 1e-9
