@@ -65,3 +65,32 @@ def test_autotune_and_one_by_one(lib, cuda, tmp_path, monkeypatch):
     f = Ensemble(systems, device=cuda)
     run_one_by_one(f, 4)
     np.testing.assert_allclose(e.pos.cpu().numpy(), f.pos.cpu().numpy(), rtol=0, atol=1e-9)
+
+
+def test_ensemble_edge_systems(lib, cuda):
+    """Systems of 0, 1 and 2 particles and one with eps = 0 (the variant that gives a
+    coincident pair no term) in one ensemble beside ordinary ones: each matches its
+    own FP64 oracle trajectory (one particle drifts at constant velocity, as
+    Simulation.calculate_acceleration gives Np <= 1 no force, gravhopper.py:419-459)."""
+    from gravhopper_gb300.ensemble import Ensemble
+    systems = _systems(4, seed=5)
+    rng = np.random.default_rng(6)
+    one = {"pos": rng.normal(size=(1, 3)) * 1e-3, "vel": rng.normal(size=(1, 3)), "mass": np.ones(1) * 1e3,
+           "eps": 5e-5, "dt": 0.005}
+    empty = {"pos": np.zeros((0, 3)), "vel": np.zeros((0, 3)), "mass": np.zeros(0), "eps": 5e-5, "dt": 0.005}
+    two = {"pos": np.array([[0.0, 0.0, 0.0], [1e-3, 2e-4, 0.0]]), "vel": np.array([[0.0, 5.0, 0.0], [0.0, -5.0, 1.0]]),
+           "mass": np.array([1e4, 3e3]), "eps": 5e-5, "dt": 0.005}
+    zero_eps = dict(systems[0])
+    zero_eps["eps"] = 0.0
+    systems = [systems[1], one, empty, two, zero_eps, systems[2]]
+    ens = Ensemble(systems, device=cuda)
+    ens.run(3, use_graph=False)
+    for k, s in enumerate(systems):
+        x, v = ens.system(k)
+        if len(s["mass"]) == 0:
+            assert x.shape == (0, 3)
+            continue
+        rx, rv = oracle.dkd_run(s["pos"], s["vel"], s["mass"], s["dt"], s["eps"], 3)
+        assert np.isfinite(x).all() and np.isfinite(v).all(), k
+        assert np.abs(x - rx).max() <= 1e-6 * np.abs(rx).max(), k
+        assert np.abs(v - rv).max() <= 1e-5 * max(np.abs(rv).max(), 1e-30), k
