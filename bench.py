@@ -209,6 +209,7 @@ def main():
     eps, dt = 5e-5, 0.005
     stream = torch.cuda.current_stream()
     fp32_peak, fp64_peak = _capi.measure_fma_peaks()
+    mix_ceiling = _capi.measure_pair_mix()  # the pair's instruction mix with operands in registers
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def barrier():
@@ -305,6 +306,11 @@ def main():
                                (f"measured live: FP64 FMA chains, {fp64_peak / 1e12:.2f} T lane-op/s "
                                 f"/ {PAIR_OPS_FP64} FP64-pipe ops per pair"),
                 "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
+    if mixed:
+        # what the same 12 FMA-pipe instructions and one MUFU per pair reach with every
+        # operand in registers (gh_measure_pair_mix): the mix's own ceiling
+        roofline["mix_ceiling"] = {"value": mix_ceiling / 1e9, "unit": UNIT, "frac": achieved / (mix_ceiling / 1e9),
+                                   "of_fma_peak": mix_ceiling / 1e9 / peak}
 
     secondary, fp64 = {}, None
     if not args.no_secondary and rank == 0:

@@ -91,6 +91,7 @@ SIGNATURES = {
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),
     "gh_measure_l2_read": (_int, [_vp, _vp]),
+    "gh_measure_pair_mix": (_int, [_vp, _vp]),
     "gh_check_inv_cube": (_int, [_i64, _u64, _vp, _vp]),
     "gh_tree_stats": (_int, [_int]),
     "gh_tree_stats_read": (_int, [_vp]),
@@ -171,6 +172,14 @@ def kernel_timing_collect():
     n = ctypes.c_int64(0)
     call("gh_kernel_timing_collect", ctypes.addressof(ms), ctypes.addressof(n))
     return ms.value, n.value
+
+
+def measure_pair_mix(stream=None):
+    """Pairs per second of the mixed direct sum's pair arithmetic with operands in
+    registers on the current device (the instruction mix's ceiling)."""
+    p = ctypes.c_double(0.0)
+    call("gh_measure_pair_mix", ctypes.addressof(p), stream_handle(stream))
+    return p.value
 
 
 def measure_l2_read(stream=None):

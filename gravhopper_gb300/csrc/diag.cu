@@ -192,7 +192,77 @@ __global__ void __launch_bounds__(256)
   }
 }
 
+// The mixed direct sum's pair arithmetic with every operand in registers: per pair 3
+// subtractions, 3 FMAs for r^2 + eps^2, one MUFU rsqrt, 3 multiplies and 3 FMAs into
+// the accumulators (12 FMA-pipe instructions and one MUFU), MIX_R targets per thread,
+// the "source" rotated through registers; no memory in the loop.  Its pairs per second
+// are the ceiling that mix reaches on this GPU, below the pure FMA-chain peak.
+constexpr int MIX_THREADS = 512, MIX_R = 4, MIX_UNROLL = 4;
+
+__global__ void __launch_bounds__(MIX_THREADS, 1) pair_mix_kernel(int iters, float seed, float* out) {
+  float sx[MIX_R], sy[MIX_R], sz[MIX_R], ax[MIX_R], ay[MIX_R], az[MIX_R];
+#pragma unroll
+  for (int r = 0; r < MIX_R; r++) {
+    sx[r] = seed * (threadIdx.x + r);
+    sy[r] = seed * ((float)threadIdx.x - r);
+    sz[r] = seed * (r + 1);
+    ax[r] = ay[r] = az[r] = 0.f;
+  }
+  float4 a = make_float4(seed, 2.f * seed, 3.f * seed, 1.f);
+  const float e2 = 1e-6f;
+  for (int k = 0; k < iters; k++) {
+#pragma unroll
+    for (int u = 0; u < MIX_UNROLL; u++) {
+#pragma unroll
+      for (int r = 0; r < MIX_R; r++) {
+        const float dx = a.x - sx[r], dy = a.y - sy[r], dz = a.z - sz[r];
+        const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, e2)));
+        const float ri = rsqrt_approx(r2);
+        const float sc = (a.w * ri) * (ri * ri);
+        ax[r] = fmaf(sc, dx, ax[r]);
+        ay[r] = fmaf(sc, dy, ay[r]);
+        az[r] = fmaf(sc, dz, az[r]);
+      }
+      a = make_float4(a.y, a.z, a.x + 1e-3f, a.w);  // the next source
+    }
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int r = 0; r < MIX_R; r++) s += ax[r] + ay[r] + az[r];
+  if (s == 12345.678f) out[0] = s;
+}
+
 }  // namespace gh
+
+extern "C" int gh_measure_pair_mix(double* pairs_per_s, void* stream) {
+  using namespace gh;
+  clear_error();
+  if (!pairs_per_s) return set_error(GH_ERR_ARG, "pair mix: null output");
+  cudaStream_t st = (cudaStream_t)stream;
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  static Buffer sink;
+  GH_TRY(ensure(sink, 64));
+  const int iters = 1 << 12, blocks = di.num_sms;
+  cudaEvent_t e0, e1;
+  GH_CUDA_TRY(cudaEventCreate(&e0));
+  GH_CUDA_TRY(cudaEventCreate(&e1));
+  float best = 1e30f;
+  for (int rep = 0; rep < 3; rep++) {
+    GH_CUDA_TRY(cudaEventRecord(e0, st));
+    pair_mix_kernel<<<blocks, MIX_THREADS, 0, st>>>(iters, 1e-3f, (float*)sink.ptr);
+    GH_LAUNCH_CHECK();
+    GH_CUDA_TRY(cudaEventRecord(e1, st));
+    GH_CUDA_TRY(cudaEventSynchronize(e1));
+    float ms = 0.f;
+    GH_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+    if (rep > 0 && ms < best) best = ms;  // first launch is warm-up
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *pairs_per_s = (double)blocks * MIX_THREADS * iters * MIX_UNROLL * MIX_R / (best * 1e-3);
+  return GH_OK;
+}
 
 extern "C" int gh_check_inv_cube(int64_t n, uint64_t seed, long long* wrong_fallback, void* stream) {
   using namespace gh;

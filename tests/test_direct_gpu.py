@@ -115,6 +115,10 @@ def test_throughput_probes(lib, cuda):
     assert 1e12 < f32 < 1e15 and 1e10 < f64 < f32
     l2 = _capi.measure_l2_read()
     assert 1e12 < l2 < 1e15
+    # the pair's instruction mix (12 FMA-pipe instructions + 1 MUFU) stays below the
+    # FMA-chain peak / 12
+    mix = _capi.measure_pair_mix()
+    assert 1e11 < mix < 1.05 * f32 / 12
 
 
 def test_integer_pipe_inverse_cube_matches_ieee(lib, cuda):
