@@ -66,6 +66,7 @@ SIGNATURES = {
     "gh_last_error": (ctypes.c_char_p, []),
     "gh_version": (_int, []),
     "gh_launch_count": (_i64, []),
+    "gh_trace": (_int, [_int]),
     "gh_direct_summation": (_int, [_vp, _vp, _i64, _dbl, _vp]),
     "gh_direct_summation_position": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _vp]),
     "gh_direct_host": (_int, [_vp, _vp, _i64, _vp, _i64, _dbl, _int, _vp]),
@@ -95,6 +96,7 @@ SIGNATURES = {
     "gh_check_inv_cube": (_int, [_i64, _u64, _vp, _vp]),
     "gh_tree_stats": (_int, [_int]),
     "gh_tree_stats_read": (_int, [_vp]),
+    "gh_tree_validate": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_debug_inject": (_int, [_int, _i64]),
     "gh_debug_sort_stall": (_int, [_i64, _vp]),
 }
@@ -224,3 +226,20 @@ def sort_stall(wait_ns: int):
     t = ctypes.c_int64(0)
     rc = load().gh_debug_sort_stall(int(wait_ns), ctypes.addressof(t))
     return int(rc), int(t.value)
+
+
+def tree_validate(pos, mass, eps, stream=None):
+    """Invariant counts of the octree of device tensors (pos, mass): cells, leaves and
+    the violations listed in gh_tree_validate (all zero for a sound tree)."""
+    out = (ctypes.c_int64 * 9)()
+    call("gh_tree_validate", ptr(pos), ptr(mass), int(pos.shape[0]), float(eps), ctypes.addressof(out),
+         stream_handle(stream))
+    keys = ("cells", "leaves", "bad_skip", "bad_children", "over_8_children", "bad_mass", "com_outside",
+            "bad_record", "bad_root")
+    return dict(zip(keys, (int(v) for v in out)))
+
+
+def trace(enable):
+    """NVTX ranges around the engine's entry points, builds, walks and steps on (True)
+    or off (False)."""
+    call("gh_trace", 1 if enable else 0)

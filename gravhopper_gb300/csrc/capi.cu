@@ -40,6 +40,7 @@ static int host_call(HostKind kind, const double* pos, const double* mass, int64
   if (n_out == 0) return GH_OK;
   if (!out || (np > 0 && (!pos || !mass)))
     return set_error(GH_ERR_ARG, "null host buffer");
+  Trace tr(kind == HK_DIRECT ? "gh host direct sum" : "gh host tree force");
   std::lock_guard<std::mutex> lk(g_stage_mu);
   HostStage* s = nullptr;
   GH_TRY(stage_for_device(&s));
@@ -109,6 +110,7 @@ int gh_tree_force_position(const double* pos, const double* mass, int64_t np, co
 int gh_tree_dev(const double* pos, const double* mass, int64_t np, const double* force_pos, int64_t nf,
                 double eps, double theta, int precision, double* acc, void* stream) {
   clear_error();
+  Trace tr("gh_tree_dev");
   return tree_force(pos, mass, np, force_pos, nf, eps, theta, precision, acc, (cudaStream_t)stream);
 }
 
@@ -120,6 +122,7 @@ int gh_direct_host(const double* pos, const double* mass, int64_t np, const doub
 int gh_direct_dev(const double* pos, const double* mass, int64_t np, const double* force_pos,
                   int64_t nf, double eps, int precision, double* acc, void* stream) {
   clear_error();
+  Trace tr("gh_direct_dev");
   return direct_force(pos, mass, np, force_pos, nf, eps, precision, acc, (cudaStream_t)stream);
 }
 
@@ -127,6 +130,7 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
                double dt, double eps, int algorithm, int precision, double theta,
                double* hist_pos, double* hist_vel, int64_t hist_stride, void* stream) {
   clear_error();
+  Trace tr("gh_run_dkd");
   if (np < 0 || nsteps < 0) return set_error(GH_ERR_ARG, "negative np or nsteps");
   if (algorithm != GH_ALGO_DIRECT && algorithm != GH_ALGO_TREE)
     return set_error(GH_ERR_ARG, "unknown algorithm %d", algorithm);

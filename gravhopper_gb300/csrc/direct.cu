@@ -424,6 +424,7 @@ int direct_run(double* x, double* v, const double* mass, int64_t np, int64_t nst
     GH_LAUNCH_CHECK();
   }
   for (int64_t s = 0; s < nsteps; s++) {
+    Trace step("direct dkd step");
     const int cur = (int)(s & 1), nxt = cur ^ 1;
     EpiDKD epi;
     epi.x = x;

@@ -106,6 +106,17 @@ int ensure(Buffer& b, size_t bytes);
 // when a fault of this kind is pending.
 bool inject_take(int fault);
 
+// Optional NVTX ranges (gh_trace): a named range over a scope of host code, visible to
+// NVTX-aware tools (Nsight Compute's --nvtx filters, Nsight Systems); no-ops while off.
+void trace_push(const char* name);
+void trace_pop();
+struct Trace {
+  explicit Trace(const char* name) { trace_push(name); }
+  ~Trace() { trace_pop(); }
+  Trace(const Trace&) = delete;
+  Trace& operator=(const Trace&) = delete;
+};
+
 struct DeviceInfo {
   int device = -1;
   int num_sms = 0;

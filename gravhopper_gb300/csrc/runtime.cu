@@ -8,9 +8,28 @@
 #include <utility>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "gh_common.cuh"
 
 namespace gh {
+
+// NVTX ranges, off by default (gh_trace).  The ranges are per host thread; a range is
+// pushed and popped on the same thread by the Trace guard.
+static std::atomic<bool> g_trace{false};
+static thread_local int g_trace_depth = 0;
+
+void trace_push(const char* name) {
+  if (!g_trace.load(std::memory_order_relaxed)) return;
+  nvtxRangePushA(name);
+  g_trace_depth++;
+}
+
+void trace_pop() {
+  if (g_trace_depth == 0) return;  // tracing was off when this scope opened
+  nvtxRangePop();
+  g_trace_depth--;
+}
 
 static thread_local char g_last_error[1024] = "";
 static std::atomic<long long> g_launches{0};
@@ -123,6 +142,12 @@ const char* gh_last_error(void) { return gh::g_last_error; }
 int gh_version(void) { return GH_VERSION; }
 
 int64_t gh_launch_count(void) { return (int64_t)gh::g_launches.load(); }
+
+int gh_trace(int enable) {
+  gh::clear_error();
+  gh::g_trace.store(enable != 0);
+  return GH_OK;
+}
 
 int gh_debug_inject(int fault, int64_t count) {
   gh::clear_error();

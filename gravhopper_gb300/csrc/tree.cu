@@ -897,6 +897,7 @@ constexpr int64_t TGT_SORT_MIN = 8192;
 
 static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t n, double eps,
                       cudaStream_t st, BuiltTree* out, const double* tpos = nullptr, int64_t nt = 0) {
+  Trace tr("tree build");
   const bool sort_targets = tpos != nullptr && nt >= TGT_SORT_MIN;
   if (sort_targets && nt > (1LL << 31))
     return set_error(GH_ERR_ARG, "tree: at most 2^31 target points (got %lld)", (long long)nt);
@@ -1065,6 +1066,7 @@ template <class Epi>
 static int tree_walk(TreeWS& ws, const BuiltTree& bt, const double* tpos, const uint32_t* order, int64_t nt,
                      double eps, double theta, int precision, const Epi& epi, cudaStream_t st) {
   if (nt == 0) return GH_OK;
+  Trace tr("tree walk");
   const double eps2 = eps * eps;
   // theta <= 0 or NaN: the prefilter opens every cell and accepts none; below 1e-3
   // it decides nothing (every internal cell takes the exact test)
@@ -1147,6 +1149,7 @@ int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nstep
   GH_TRY(ensure(ws.xh[1], (size_t)np * 3 * sizeof(double)));
   GH_TRY(drift_prepare_f64(x, v, np, dt, (double*)ws.xh[0].ptr, st));
   for (int64_t s = 0; s < nsteps; s++) {
+    Trace step("tree dkd step");
     const int cur = (int)(s & 1), nxt = cur ^ 1;
     const double* xh = (const double*)ws.xh[cur].ptr;
     BuiltTree bt;
@@ -1171,6 +1174,87 @@ int tree_run(double* x, double* v, const double* mass, int64_t np, int64_t nstep
 }
 
 }  // namespace gh
+
+// ---------------------------------------------------------------------------
+// Invariant check of a built tree (gh_tree_validate)
+// ---------------------------------------------------------------------------
+// out: [0] leaves, [1] skip index out of range, [2] children that do not tile their
+// cell's subtree, [3] cells with more than 8 child cells, [4] cell mass not the sum of
+// its children's, [5] a child's centre of mass outside its cell, [6] walk record not
+// matching the FP64 cell, [7] root subtree not the whole preorder.
+namespace gh {
+__global__ void tree_validate_kernel(const WalkRec* __restrict__ R, const dvec4* __restrict__ C,
+                                     const dvec4* __restrict__ M, int nnodes, unsigned long long* __restrict__ out) {
+  for (int k = blockIdx.x * blockDim.x + threadIdx.x; k < nnodes; k += gridDim.x * blockDim.x) {
+    const int nx = __float_as_int(R[k].L.w);
+    if (k == 0 && nx != nnodes) atomicAdd(&out[7], 1ull);
+    if (nx <= k || nx > nnodes) {
+      atomicAdd(&out[1], 1ull);
+      continue;
+    }
+    const dvec4 Mk = M[k];
+    if (nx == k + 1) {  // leaf: its record is its particle
+      atomicAdd(&out[0], 1ull);
+      const float4 A = R[k].A;
+      if (A.x != (float)Mk.x || A.y != (float)Mk.y || A.z != (float)Mk.z || R[k].O.w != (float)Mk.w)
+        atomicAdd(&out[6], 1ull);
+      continue;
+    }
+    const dvec4 Ck = C[k];
+    const float4 A = R[k].A;
+    if (A.x != (float)Ck.x || A.y != (float)Ck.y || A.z != (float)Ck.z || A.w != (float)(Ck.w * Ck.w) ||
+        R[k].O.w != (float)Mk.w)
+      atomicAdd(&out[6], 1ull);
+    // children: k + 1, then each one's skip index, up to this cell's skip index (at most 8
+    // steps are taken; a ninth child counts as a violation)
+    const double half = 0.5 * Ck.w * (1.0 + 1e-12);
+    double msum = 0.0;
+    int c = k + 1, kids = 0;
+    while (c < nx && kids <= 8) {
+      const dvec4 Mc = M[c];
+      msum += Mc.w;
+      if (fabs(Mc.x - Ck.x) > half || fabs(Mc.y - Ck.y) > half || fabs(Mc.z - Ck.z) > half)
+        atomicAdd(&out[5], 1ull);
+      const int cn = __float_as_int(R[c].L.w);
+      if (cn <= c || cn > nx) break;
+      c = cn;
+      kids++;
+    }
+    if (kids > 8) atomicAdd(&out[3], 1ull);
+    else if (c != nx) atomicAdd(&out[2], 1ull);
+    if (!(fabs(msum - Mk.w) <= 1e-12 * fabs(Mk.w))) atomicAdd(&out[4], 1ull);
+  }
+}
+}  // namespace gh
+
+extern "C" int gh_tree_validate(const double* pos, const double* mass, int64_t np, double eps, int64_t* out,
+                                void* stream) {
+  using namespace gh;
+  clear_error();
+  if (!out) return set_error(GH_ERR_ARG, "tree validate: null output");
+  if (np <= 0) return set_error(GH_ERR_ARG, "tree validate: no particles");
+  if (!pos || !mass) return set_error(GH_ERR_ARG, "null buffer");
+  cudaStream_t st = (cudaStream_t)stream;
+  std::lock_guard<std::recursive_mutex> lk(g_tree_mu);
+  DeviceInfo di;
+  GH_TRY(device_info(&di));
+  TreeWS& ws = g_tree[di.device];
+  BuiltTree bt;
+  GH_TRY(tree_build(ws, pos, mass, np, eps, st, &bt));
+  static Buffer counts[64];
+  GH_TRY(ensure(counts[di.device], 8 * sizeof(unsigned long long)));
+  unsigned long long* dc = (unsigned long long*)counts[di.device].ptr;
+  GH_CUDA_TRY(cudaMemsetAsync(dc, 0, 8 * sizeof(unsigned long long), st));
+  NodeArrays na = node_arrays(ws);
+  tree_validate_kernel<<<2 * di.num_sms, 256, 0, st>>>(na.R, na.C, na.M, bt.nnodes, dc);
+  GH_LAUNCH_CHECK();
+  unsigned long long h[8];
+  GH_CUDA_TRY(cudaMemcpyAsync(h, dc, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GH_CUDA_TRY(cudaStreamSynchronize(st));
+  out[0] = bt.nnodes;
+  for (int k = 0; k < 8; k++) out[k + 1] = (int64_t)h[k];
+  return GH_OK;
+}
 
 extern "C" int gh_tree_stats(int enable) {
   using namespace gh;

@@ -21,6 +21,8 @@ plain numbers in kpc, km/s, Msun, Myr.
 """
 from __future__ import annotations
 
+import time
+
 import numpy as np
 
 from . import ics as _ics
@@ -166,8 +168,15 @@ class Simulation(object):
 
     # ---- running (gravhopper.py:293-342) ---------------------------------------
     def run(self, N=1):
-        """Run N timesteps; initialises on the first call, continues afterwards."""
+        """Run N timesteps; initialises on the first call, continues afterwards.
+        Afterwards run_stats() describes this call (steps, wall time, throughput)."""
         N = int(N)
+        t_start = time.perf_counter()
+        host = self._has_extra_forces()
+        self._run(N)
+        self._record_run(N, time.perf_counter() - t_start, host)
+
+    def _run(self, N):
         if not self.running:
             self.init_run(N)
         else:
@@ -182,6 +191,23 @@ class Simulation(object):
                 self._times[self.timestep] = self._times[self.timestep - 1] + self._dt()
             return
         self._run_device(N)
+
+    def _record_run(self, N, seconds, host):
+        np_ = int(self.Np)
+        pairs = np_ * (np_ - 1) if self.params["algorithm"] == "direct" else None
+        self._last_run = {"steps": max(N, 0), "particles": np_, "seconds": seconds,
+                          "algorithm": self.params["algorithm"], "precision": self.params["precision"],
+                          "path": "host steps (external forces)" if host else "device",
+                          "particle_steps_per_s": np_ * max(N, 0) / seconds if seconds > 0 else None,
+                          "pairs_per_s": (pairs * max(N, 0) / seconds if pairs is not None and seconds > 0
+                                          else None)}
+
+    def run_stats(self):
+        """Statistics of the last run() call: steps, particles, wall-clock seconds
+        (history copies included), particle steps per second and, for the direct sum,
+        pair interactions per second; algorithm, precision and whether the steps ran
+        on the device or as host steps (external forces).  None before any run."""
+        return None if getattr(self, "_last_run", None) is None else dict(self._last_run)
 
     def _has_extra_forces(self):
         return bool(self.extra_force_functions or self.extra_timedependent_force_functions

@@ -49,6 +49,9 @@ const char* gh_last_error(void);
 int gh_version(void);
 /* Number of kernels this library has launched since load (all threads). */
 int64_t gh_launch_count(void);
+/* Enables (1) or disables (0) NVTX ranges around the library's calls, leapfrog steps,
+ * tree builds and walks, for NVTX-aware profilers (no counterpart in the reference). */
+int gh_trace(int enable);
 
 /* ---- host-buffer drop-ins for the reference module gravhopper._jbgrav --------- */
 
@@ -225,6 +228,16 @@ int gh_measure_l2_read(double* bytes_per_s, void* stream);
  * Writes the number of differing results and of in-range inputs that took the
  * native path. */
 int gh_check_inv_cube(int64_t n, uint64_t seed, long long* wrong_fallback, void* stream);
+
+/* Builds the octree of (pos, mass) (device buffers) and checks its invariants (no
+ * counterpart in the reference, whose pointer tree has none to check): out holds 9
+ * entries, out[0] the number of cells, out[1] the leaves (np when the tree is whole),
+ * then violations: out[2] skip indices out of range, out[3] children that do not tile
+ * their cell's subtree, out[4] cells with more than 8 child cells, out[5] cell masses
+ * that are not the sum of their children's (1e-12 relative), out[6] children whose
+ * centre of mass lies outside their cell, out[7] walk records that do not match the
+ * FP64 cells, out[8] a root whose subtree is not the whole preorder.  Synchronises. */
+int gh_tree_validate(const double* pos, const double* mass, int64_t np, double eps, int64_t* out, void* stream);
 
 /* Enables (1) or disables (0) the tree-walk counters (no counterpart in the
  * reference, which counts nothing).  While enabled every walk adds, over its warps,

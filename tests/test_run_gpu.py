@@ -157,3 +157,28 @@ def test_momentum_diagnostics_conserved(lib, cuda, precision):
     tol = 1e-12 if precision == "fp64" else 1e-6
     assert float(torch.linalg.norm(p1 - p0)) <= tol * scale_p
     assert float(torch.linalg.norm(l1 - l0)) <= tol * scale_l
+
+
+def test_run_stats_and_tracing_leave_results_alone(golden, lib, cuda):
+    """run_stats() reports the last run() call; NVTX ranges (gh_trace) change no bit
+    of a run (without an attached tool the ranges are no-ops)."""
+    from gravhopper_gb300 import _capi
+    from gravhopper_gb300.gravhopper import Simulation
+    ic = {"pos": golden["plummer_pos"], "vel": golden["plummer_vel"], "mass": golden["plummer_mass"]}
+    runs = []
+    for trace in (False, True):
+        sim = Simulation(dt=0.005, eps=5e-5, algorithm="direct")
+        assert sim.run_stats() is None
+        sim.add_IC(ic)
+        _capi.trace(trace)
+        try:
+            sim.run(10)
+        finally:
+            _capi.trace(False)
+        runs.append(sim.positions[10].copy())
+        st = sim.run_stats()
+        n = len(ic["mass"])
+        assert st["steps"] == 10 and st["particles"] == n and st["path"] == "device"
+        assert st["seconds"] > 0 and np.isclose(st["particle_steps_per_s"], 10 * n / st["seconds"])
+        assert np.isclose(st["pairs_per_s"], 10 * n * (n - 1) / st["seconds"])
+    np.testing.assert_array_equal(runs[0], runs[1])

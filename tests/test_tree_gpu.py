@@ -266,3 +266,53 @@ def test_tree_many_target_points_any_order(lib, cuda, precision, rms_tol, max_to
                             precision=precision).cpu().numpy()
     assert np.isfinite(got).all()
     check(got, oracle.tree_force_position(ic["pos"], ic["mass"], fp, eps, 0.7), rms_tol, max_tol)
+
+
+def _validate(pos, m, eps):
+    import torch
+
+    from gravhopper_gb300 import _capi
+    d = torch.device("cuda:0")
+    return _capi.tree_validate(torch.as_tensor(np.ascontiguousarray(pos), dtype=torch.float64, device=d),
+                               torch.as_tensor(np.ascontiguousarray(m), dtype=torch.float64, device=d), eps)
+
+
+def _tree_cases():
+    from gravhopper_gb300 import ics
+    rng = np.random.default_rng(21)
+    g = np.arange(12) / 8.0
+    lattice = np.stack(np.meshgrid(g, g, g, indexing="ij"), -1).reshape(-1, 3)
+    base = rng.uniform(-1, 1, size=(50, 3))
+    deep = np.concatenate([base, base + 1e-13 * rng.normal(size=base.shape)])
+    clumps = (rng.uniform(-1, 1, size=(30, 1, 3)) + 1e-8 * rng.uniform(0, 1, size=(30, 100, 3))).reshape(-1, 3)
+    pl = ics.plummer(5000, seed=8)
+    return {"one": (np.array([[0.5, -1.0, 2.0]]), np.array([3.0])),
+            "two": (np.array([[0.0, 0.0, 0.0], [1.0, 2.0, 3.0]]), np.array([1.0, 2.0])),
+            "lattice": (lattice, np.ones(len(lattice))),
+            "deep": (deep, rng.uniform(1, 2, size=len(deep))),
+            "clumps": (clumps, rng.uniform(1, 2, size=len(clumps))),
+            "plummer": (pl["pos"], pl["mass"])}
+
+
+@pytest.mark.parametrize("case", ["one", "two", "lattice", "deep", "clumps", "plummer"])
+def test_tree_invariants_match_reference_cell_count(lib, cuda, case):
+    """gh_tree_validate on trees the reference builds too: one leaf per particle, skip
+    indices that tile every cell's subtree with at most 8 children, cell masses equal
+    to their children's sums, every child's centre of mass inside its cell, walk
+    records equal to the FP64 cells, and as many cells as the reference's tree, which
+    inserts one particle at a time (gravoct_add_particle, _jbgrav.c:387-439)."""
+    pos, m = _tree_cases()[case]
+    v = _validate(pos, m, 1e-3)
+    _, ncells = oracle.tree_force(pos, m, 1e-3, 0.0, return_nodes=True)
+    assert v["leaves"] == len(m) and v["cells"] == ncells, v
+    assert all(v[k] == 0 for k in v if k not in ("cells", "leaves")), v
+
+
+def test_tree_invariants_large(lib, cuda):
+    """The same invariants at 1M particles of a Hernquist disk (the tree-force bench
+    workload) and with target points sorted into the build."""
+    from gravhopper_gb300 import ics
+    ic = ics.hernquist_disk(1 << 20, seed=1)
+    v = _validate(ic["pos"], ic["mass"], 5e-5)
+    assert v["leaves"] == 1 << 20 and v["cells"] > 1 << 20, v
+    assert all(v[k] == 0 for k in v if k not in ("cells", "leaves")), v
