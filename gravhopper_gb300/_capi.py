@@ -97,6 +97,8 @@ SIGNATURES = {
     "gh_tree_stats": (_int, [_int]),
     "gh_tree_stats_read": (_int, [_vp]),
     "gh_tree_validate": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
+    "gh_dkd_drift": (_int, [_vp, _vp, _i64, _dbl, _vp, _vp]),
+    "gh_dkd_kick_drift": (_int, [_vp, _vp, _vp, _vp, _i64, _dbl, _vp, _vp]),
     "gh_debug_inject": (_int, [_int, _i64]),
     "gh_debug_sort_stall": (_int, [_i64, _vp]),
 }

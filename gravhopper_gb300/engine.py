@@ -80,6 +80,44 @@ def run_dkd(pos, vel, mass, nsteps, dt, eps, algorithm="direct", precision="fp64
     return (hp, hv) if hist_stride > 0 else None
 
 
+def dkd_drift(pos, vel, dt, out=None, stream=None):
+    """First drift of a leapfrog step: ``pos + ((0.5 vel) dt) F`` (kpc; F = km Myr/s
+    in kpc), into ``out`` (a new tensor by default; may be ``pos``)."""
+    _check(pos, "pos", 3)
+    _check(vel, "vel", 3)
+    if vel.shape[0] != pos.shape[0]:
+        raise ValueError("pos and vel have different lengths")
+    if out is None:
+        out = torch.empty_like(pos)
+    _check(out, "out", 3)
+    _capi.call("gh_dkd_drift", _capi.ptr(pos), _capi.ptr(vel), pos.shape[0], float(dt), _capi.ptr(out),
+               _capi.stream_handle(stream))
+    return out
+
+
+def dkd_kick_drift(pos_half, vel, acc, acc_ext, dt, out=None, stream=None):
+    """Kick and second drift of a leapfrog step: ``vel += ((acc ACC) + acc_ext) dt`` in
+    place, then ``out = pos_half + ((0.5 vel) dt) F``.  ``acc`` is the N-body
+    acceleration in code units or None (no N-body force); ``acc_ext`` the external
+    acceleration in km/s/Myr or None."""
+    _check(pos_half, "pos_half", 3)
+    _check(vel, "vel", 3)
+    n = pos_half.shape[0]
+    for t, name in ((acc, "acc"), (acc_ext, "acc_ext")):
+        if t is not None:
+            _check(t, name, 3)
+            if t.shape[0] != n:
+                raise ValueError(f"{name} and pos_half have different lengths")
+    if vel.shape[0] != n:
+        raise ValueError("pos_half and vel have different lengths")
+    if out is None:
+        out = torch.empty_like(pos_half)
+    _check(out, "out", 3)
+    _capi.call("gh_dkd_kick_drift", _capi.ptr(pos_half), _capi.ptr(vel), _capi.ptr(acc), _capi.ptr(acc_ext), n,
+               float(dt), _capi.ptr(out), _capi.stream_handle(stream))
+    return out
+
+
 def direct_vjp(pos, mass, eps, cot, precision="fp64", grad_pos=None, grad_mass=None, stream=None):
     """Vector-Jacobian product of the direct-sum self-acceleration (code units).
 

@@ -62,6 +62,33 @@ class ExternalPackageException(GravHopperException):
         print(msg)
 
 
+class DeviceForce(object):
+    """An external force evaluated on the GPU: ``fn`` takes CUDA float64 tensors
+    (positions in kpc, velocities in km/s; time as a float in Myr) and returns the
+    acceleration in km/s/Myr as a tensor of shape (N,3) or one that broadcasts to it.
+    Simulation.run calls it on the device-resident state, with no host copies.  Called
+    with host arrays (Simulation.calculate_acceleration), it moves them to the current
+    CUDA device and returns a numpy array.  No counterpart in the reference, whose
+    external forces are host functions (gravhopper.py:603-845)."""
+
+    def __init__(self, fn):
+        if not callable(fn):
+            raise ExternalPackageException("A device force must be callable.")
+        self.fn = fn
+
+    def __call__(self, pos, *rest):
+        import torch
+        dev = torch.device("cuda", torch.cuda.current_device())
+
+        def to_dev(a, unit):
+            return torch.as_tensor(np.ascontiguousarray(U.value(a, unit), dtype=np.float64), device=dev)
+        args = list(rest)
+        if len(args) == 2:  # (time, args): a scalar; (vel, args): an (N,3) array
+            args[0] = float(U.value(args[0], U.TIME)) if np.ndim(args[0]) == 0 else to_dev(args[0], U.VELOCITY)
+        out = self.fn(to_dev(pos, U.LENGTH), *args)
+        return U.quantity(torch.as_tensor(out).cpu().numpy(), U.ACCEL)
+
+
 def _default(q_astropy, plain):
     return q_astropy() if U.HAVE_ASTROPY else plain
 
@@ -185,10 +212,7 @@ class Simulation(object):
             self._vel = np.concatenate((self._vel, np.zeros((N, self.Np, 3))), axis=0)
             self._times = np.concatenate((self._times, np.zeros(N)), axis=0)
         if self._has_extra_forces():
-            for _ in range(N):
-                self.timestep += 1
-                self.perform_timestep()
-                self._times[self.timestep] = self._times[self.timestep - 1] + self._dt()
+            self._run_device_external(N)
             return
         self._run_device(N)
 
@@ -197,7 +221,7 @@ class Simulation(object):
         pairs = np_ * (np_ - 1) if self.params["algorithm"] == "direct" else None
         self._last_run = {"steps": max(N, 0), "particles": np_, "seconds": seconds,
                           "algorithm": self.params["algorithm"], "precision": self.params["precision"],
-                          "path": "host steps (external forces)" if host else "device",
+                          "path": "device, external forces" if host else "device",
                           "particle_steps_per_s": np_ * max(N, 0) / seconds if seconds > 0 else None,
                           "pairs_per_s": (pairs * max(N, 0) / seconds if pairs is not None and seconds > 0
                                           else None)}
@@ -205,8 +229,8 @@ class Simulation(object):
     def run_stats(self):
         """Statistics of the last run() call: steps, particles, wall-clock seconds
         (history copies included), particle steps per second and, for the direct sum,
-        pair interactions per second; algorithm, precision and whether the steps ran
-        on the device or as host steps (external forces).  None before any run."""
+        pair interactions per second; algorithm, precision and whether external forces
+        were evaluated each step.  None before any run."""
         return None if getattr(self, "_last_run", None) is None else dict(self._last_run)
 
     def _has_extra_forces(self):
@@ -259,6 +283,85 @@ class Simulation(object):
         for k in range(t0 + 1, t0 + N + 1):
             self._times[k] = self._times[k - 1] + dt
         self.timestep = t0 + N
+
+    def _force_fn(self):
+        from . import engine
+        p = self.params
+        if p["algorithm"] == "direct":
+            return lambda x, m, out: engine.direct_force(x, m, self._eps(), precision=p["precision"], out=out)
+        if p["algorithm"] == "tree":
+            return lambda x, m, out: engine.tree_force(x, m, self._eps(), p["theta"], precision=p["precision"],
+                                                       out=out)
+        raise UnknownAlgorithmException()
+
+    def _run_device_external(self, N):
+        """Steps with external forces, state resident on the device: per step the first
+        drift, the N-body force and the external accelerations (device forces on the
+        device; host functions on a copy of the half-drifted positions, their result
+        copied back), then the kick and second drift, and the snapshot copied into the
+        history.  The same arithmetic and order as perform_timestep with
+        calculate_acceleration (gravhopper.py:405-473)."""
+        import torch
+
+        from . import engine
+        if N <= 0:
+            return
+        force = self._force_fn()
+        dev = torch.device("cuda", torch.cuda.current_device())
+        t0 = self.timestep
+        dt = self._dt()
+        x = torch.from_numpy(np.ascontiguousarray(self._pos[t0])).to(dev)
+        v = torch.from_numpy(np.ascontiguousarray(self._vel[t0])).to(dev)
+        m = torch.from_numpy(np.ascontiguousarray(self._mass)).to(dev)
+        xh = torch.empty_like(x)
+        acc = torch.empty_like(x) if self.Np > 1 else None
+        ext = torch.empty_like(x)
+        host = [fn for fns in self._external_lists() for fn, _ in fns if not isinstance(fn, DeviceForce)]
+        xh_host = torch.empty((self.Np, 3), dtype=torch.float64, pin_memory=True) if host else None
+        for k in range(N):
+            t = t0 + k + 1
+            engine.dkd_drift(x, v, dt, out=xh)
+            if acc is not None:
+                force(xh, m, acc)
+            self._external_on_device(xh, v, ext, xh_host, t)
+            engine.dkd_kick_drift(xh, v, acc, ext, dt, out=x)
+            torch.from_numpy(self._pos[t]).copy_(x)
+            torch.from_numpy(self._vel[t]).copy_(v)
+            self._times[t] = self._times[t - 1] + dt
+            self.timestep = t
+
+    def _external_lists(self):
+        return (self.extra_force_functions, self.extra_timedependent_force_functions,
+                self.extra_velocitydependent_force_functions)
+
+    def _external_on_device(self, xh, v, ext, xh_host, t):
+        """ext = 0 + each registered force in the reference's order (gravhopper.py:462-473),
+        at the half-drifted positions xh, time t_(t-1) + dt/2 and the step's starting
+        velocities."""
+        import torch
+        kick_time = self._times[t - 1] + 0.5 * self._dt()
+        ext.zero_()
+        pos_host = None
+        for kind, fns in zip(("pos", "time", "vel"), self._external_lists()):
+            for fn, args in fns:
+                if isinstance(fn, DeviceForce):
+                    extra = (xh,) if kind == "pos" else (xh, kick_time) if kind == "time" else (xh, v)
+                    r = fn.fn(*extra, args)
+                    if not isinstance(r, torch.Tensor) or r.device != ext.device:
+                        raise ExternalPackageException("A device force must return a tensor on the state's device.")
+                    ext.add_(r.to(torch.float64))
+                    continue
+                if pos_host is None:
+                    xh_host.copy_(xh)
+                    pos_host = U.quantity(xh_host.numpy(), U.LENGTH)
+                if kind == "pos":
+                    r = fn(pos_host, args)
+                elif kind == "time":
+                    r = fn(pos_host, U.quantity(kick_time, U.TIME), args)
+                else:
+                    r = fn(pos_host, U.quantity(self._vel[t - 1], U.VELOCITY), args)
+                r = np.asarray(U.value(r, U.ACCEL, "acceleration"), dtype=np.float64)
+                ext.add_(torch.from_numpy(np.ascontiguousarray(r)).to(ext.device))
 
     def _copy_history(self, hp, hv, ready, stream, first):
         import torch
@@ -341,35 +444,39 @@ class Simulation(object):
         return ext
 
     # ---- external forces (gravhopper.py:603-845): plain callables -----------------
-    def add_external_force(self, fn, args=None, agama_units=None):
+    # ``device=True`` (not in the reference) registers a DeviceForce: fn takes and
+    # returns CUDA tensors and runs on the device-resident state.
+    @staticmethod
+    def _external(fn, device):
+        if device:
+            return fn if isinstance(fn, DeviceForce) else DeviceForce(fn)
+        if not callable(fn):
+            raise ExternalPackageException("Only callables are supported as external forces here.")
+        return fn
+
+    def add_external_force(self, fn, args=None, agama_units=None, device=False):
         """Add a position-dependent force ``fn(pos, args)`` (km/s/Myr when unitless)."""
         if isinstance(fn, list):
             for item in fn:
-                self.add_external_force(item, args)
+                self.add_external_force(item, args, device=device)
             return
-        if not callable(fn):
-            raise ExternalPackageException("Only callables are supported as external forces here.")
-        self.extra_force_functions.append((fn, args))
+        self.extra_force_functions.append((self._external(fn, device), args))
 
-    def add_external_timedependent_force(self, fn, agama_units=None, args=None):
+    def add_external_timedependent_force(self, fn, agama_units=None, args=None, device=False):
         """Add a time-dependent force ``fn(pos, time, args)``."""
         if isinstance(fn, list):
             for item in fn:
-                self.add_external_timedependent_force(item, args=args)
+                self.add_external_timedependent_force(item, args=args, device=device)
             return
-        if not callable(fn):
-            raise ExternalPackageException("Only callables are supported as external forces here.")
-        self.extra_timedependent_force_functions.append((fn, args))
+        self.extra_timedependent_force_functions.append((self._external(fn, device), args))
 
-    def add_external_velocitydependent_force(self, fn, args=None):
+    def add_external_velocitydependent_force(self, fn, args=None, device=False):
         """Add a velocity-dependent force ``fn(pos, vel, args)``."""
         if isinstance(fn, list):
             for item in fn:
-                self.add_external_velocitydependent_force(item, args)
+                self.add_external_velocitydependent_force(item, args, device=device)
             return
-        if not callable(fn):
-            raise ExternalPackageException("Only callables are supported as external forces here.")
-        self.extra_velocitydependent_force_functions.append((fn, args))
+        self.extra_velocitydependent_force_functions.append((self._external(fn, device), args))
 
     # ---- initial conditions (gravhopper.py:848-904) --------------------------------
     def nrows(self, array):

@@ -107,6 +107,21 @@ int gh_run_dkd(double* pos, double* vel, const double* mass, int64_t np, int64_t
                double dt, double eps, int algorithm, int precision, double theta,
                double* hist_pos, double* hist_vel, int64_t hist_stride, void* stream);
 
+/* The leapfrog step of gh_run_dkd in two launches, for runs whose acceleration has a
+ * part computed outside this library (the external forces of
+ * Simulation.calculate_extra_acceleration, gravhopper/gravhopper.py:462-473).
+ * gh_dkd_drift: pos_half = pos + ((0.5 vel) dt) F, F = km Myr/s in kpc (the first
+ * drift of Simulation.perform_timestep, gravhopper.py:405-416); all device (np,3)
+ * buffers, pos_half may be pos.  gh_dkd_kick_drift: vel += ((acc ACC) + acc_ext) dt,
+ * then pos_out = pos_half + ((0.5 vel) dt) F, with acc the N-body acceleration in code
+ * units (as gh_direct_dev and gh_tree_dev give it; NULL for none, as for np <= 1,
+ * gravhopper.py:457-458), ACC = G Msun/kpc^2 in km/s/Myr (jbgrav.py:40-48), and
+ * acc_ext the external acceleration in km/s/Myr (NULL for none): the reference's
+ * nbody + extra (gravhopper.py:459).  No FMA contraction, as in gh_run_dkd. */
+int gh_dkd_drift(const double* pos, const double* vel, int64_t np, double dt, double* pos_half, void* stream);
+int gh_dkd_kick_drift(const double* pos_half, double* vel, const double* acc, const double* acc_ext, int64_t np,
+                      double dt, double* pos_out, void* stream);
+
 /* Mixed-precision direct-sum self-force (as gh_direct_dev with force_pos == NULL and
  * GH_PREC_MIXED) that allocates no device memory.  No counterpart in the reference:
  * it is for callers that cannot let a library allocate, such as an application

@@ -182,3 +182,99 @@ def test_run_stats_and_tracing_leave_results_alone(golden, lib, cuda):
         assert st["seconds"] > 0 and np.isclose(st["particle_steps_per_s"], 10 * n / st["seconds"])
         assert np.isclose(st["pairs_per_s"], 10 * n * (n - 1) / st["seconds"])
     np.testing.assert_array_equal(runs[0], runs[1])
+
+
+def _restated_run(pos, vel, mass, steps, dt, eps, forces):
+    """Simulation.perform_timestep with calculate_acceleration (gravhopper.py:405-473)
+    in NumPy: the N-body part from the oracle, the external forces summed onto zeros in
+    registration order.  forces: list of (kind, fn, args), kind 'pos', 'time' or 'vel'."""
+    x, v, t = pos.copy(), vel.copy(), 0.0
+    for _ in range(steps):
+        xh = x + ((0.5 * v) * dt) * oracle.KMS_MYR_TO_KPC
+        nbody = (oracle.direct_summation(xh, mass, eps) * oracle.ACCEL_UNIT if len(mass) > 1
+                 else np.zeros_like(xh))
+        ext = np.zeros_like(nbody)
+        for kind in ("pos", "time", "vel"):
+            for k, fn, args in forces:
+                if k == kind:
+                    ext += (fn(xh, args) if k == "pos" else fn(xh, t + 0.5 * dt, args) if k == "time"
+                            else fn(xh, v, args))
+        v = v + (nbody + ext) * dt
+        x = xh + ((0.5 * v) * dt) * oracle.KMS_MYR_TO_KPC
+        t = t + dt
+    return x, v
+
+
+def _plummer_halo(pos, args):
+    """A Plummer-sphere pull, -k x / (r^2 + b^2)^(3/2), in +, *, / and sqrt only (correctly
+    rounded alike in NumPy and on the GPU)."""
+    xp = np if isinstance(pos, np.ndarray) else __import__("torch")
+    r2 = pos[:, 0] * pos[:, 0] + pos[:, 1] * pos[:, 1] + pos[:, 2] * pos[:, 2]  # no reduction order to differ
+    s = r2 + args["b"] * args["b"]
+    return -args["k"] * pos / (s * xp.sqrt(s))[:, None]
+
+
+def _swirl(pos, t, args):
+    return args["w"] * t * pos[:, [1, 0, 2]] * np.array([1.0, -1.0, 0.0]) if isinstance(pos, np.ndarray) else \
+        args["w"] * t * pos[:, [1, 0, 2]] * __import__("torch").tensor([1.0, -1.0, 0.0], dtype=pos.dtype,
+                                                                        device=pos.device)
+
+
+def _drag(pos, vel, args):
+    return -args["c"] * vel
+
+
+@pytest.mark.parametrize("device_forces", [False, True])
+def test_external_forces_on_device_match_restatement(golden, lib, cuda, device_forces):
+    """Position-, time- and velocity-dependent external forces, as host functions or as
+    device forces (torch on the resident state): every snapshot bit-identical to the
+    NumPy restatement of perform_timestep + calculate_acceleration."""
+    import gravhopper_gb300 as gh
+    n = 300
+    pos0, vel0, mass = golden["plummer_pos"][:n], golden["plummer_vel"][:n], golden["plummer_mass"][:n]
+    forces = [("pos", _plummer_halo, {"k": 2.0e-3, "b": 3e-3}), ("time", _swirl, {"w": 40.0}),
+              ("vel", _drag, {"c": 0.3}), ("pos", _plummer_halo, {"k": 5.0e-4, "b": 1e-2})]
+    sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct")
+    sim.add_IC({"pos": pos0, "vel": vel0, "mass": mass})
+    for kind, fn, args in forces:
+        if kind == "pos":
+            sim.add_external_force(fn, args, device=device_forces)
+        elif kind == "time":
+            sim.add_external_timedependent_force(fn, args=args, device=device_forces)
+        else:
+            sim.add_external_velocitydependent_force(fn, args, device=device_forces)
+    sim.run(5)
+    sim.run(3)  # continued run
+    x, v = _restated_run(pos0, vel0, mass, 8, 0.005, 5e-5, forces)
+    np.testing.assert_array_equal(sim.positions[8], x)
+    np.testing.assert_array_equal(sim.velocities[8], v)
+    assert sim.run_stats()["path"] == "device, external forces"
+    # the host-facing calculate_acceleration takes device forces too
+    acc = sim.calculate_acceleration(time=sim.times[8])
+    assert np.asarray(acc).shape == (n, 3) and np.isfinite(acc).all()
+
+
+def test_external_force_single_particle_and_tree(golden, lib, cuda):
+    """One particle has no N-body force (gravhopper.py:457-458) and moves in the external
+    field alone; the tree algorithm with a device force matches the same run with the
+    force as a host function bit for bit."""
+    import gravhopper_gb300 as gh
+    one = {"pos": np.array([[1e-3, 2e-3, -5e-4]]), "vel": np.array([[3.0, -1.0, 0.5]]), "mass": np.array([1e4])}
+    sim = gh.Simulation(dt=0.005, eps=5e-5, algorithm="direct")
+    sim.add_IC(one)
+    sim.add_external_force(_plummer_halo, {"k": 2.0e-3, "b": 3e-3}, device=True)
+    sim.run(6)
+    x, v = _restated_run(one["pos"], one["vel"], one["mass"], 6, 0.005, 5e-5,
+                         [("pos", _plummer_halo, {"k": 2.0e-3, "b": 3e-3})])
+    np.testing.assert_array_equal(sim.positions[6], x)
+    np.testing.assert_array_equal(sim.velocities[6], v)
+    ic = {"pos": golden["plummer_pos"], "vel": golden["plummer_vel"], "mass": golden["plummer_mass"]}
+    runs = []
+    for device in (False, True):
+        s = gh.Simulation(dt=0.005, eps=5e-5, algorithm="tree", precision="mixed")
+        s.add_IC(ic)
+        s.add_external_force(_plummer_halo, {"k": 2.0e-3, "b": 3e-3}, device=device)
+        s.run(4)
+        runs.append((s.positions[4].copy(), s.velocities[4].copy()))
+    np.testing.assert_array_equal(runs[0][0], runs[1][0])
+    np.testing.assert_array_equal(runs[0][1], runs[1][1])
