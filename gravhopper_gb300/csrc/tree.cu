@@ -711,6 +711,33 @@ __device__ __forceinline__ double rsqrt_f64(double s) {
 // FP64 with s^(-3/2) from the integer-pipe reciprocal square root (f64emu.cuh).
 // The opening decisions are the same exact ones in both forms.
 constexpr int TW_FOLD = 32;
+// FP64: a lane's accepted cells wait in a FIFO of TW_FQ entries and are evaluated in
+// rounds that run when at least TW_FQ_ROUND lanes have one waiting (or a FIFO is
+// full), so the FP64 pipe (1/74 of the FP32 rate on GB300) issues fewer partly empty
+// instructions; each lane still adds its interactions in visiting order.
+constexpr int TW_FQ = 32;
+constexpr int TW_FQ_ROUND = 28;
+
+// One FP64 interaction: the cell's monopole (nM) with s^(-3/2) on the integer pipes,
+// FP64 Newton steps outside the emulation's range.
+template <bool GUARD>
+__device__ __forceinline__ void walk_interact_f64(const dvec4* __restrict__ nM, int node, double p0, double p1,
+                                                  double p2, double eps2, double& ax, double& ay, double& az) {
+  const dvec4 M = nM[node];
+  const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
+  const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
+  if (!GUARD || s != 0.0) {
+    double y3;
+    if (!emu::rsqrt_cube(s, y3)) {
+      const double y = rsqrt_f64(s);
+      y3 = y * (y * y);
+    }
+    const double f = M.w * y3;
+    ax = fma(f, dx, ax);
+    ay = fma(f, dy, ay);
+    az = fma(f, dz, az);
+  }
+}
 
 template <bool GUARD, bool MIXED, bool STATS, class Epi>
 __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
@@ -739,6 +766,8 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
   float px = 0.f, py = 0.f, pz = 0.f;            // FP32 partial (MIXED)
   float hx = 0.f, hy = 0.f, hz = 0.f, qx = 0.f, qy = 0.f, qz = 0.f;  // two-sum hi, lo
   int pending = 0;
+  __shared__ int fq[MIXED ? 1 : TW_FQ][TW_THREADS];  // FP64: this lane's accepted cells, FIFO
+  int fq_head = 0, fq_n = 0;
   unsigned n_step = 0, n_visit = 0, n_inter = 0, n_exact = 0, n_leaf = 0, n_chain = 0;  // walk counters (STATS)
   int skip = valid ? 0 : 0x7fffffff;
   int node = __reduce_min_sync(0xffffffffu, skip);
@@ -800,25 +829,26 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
           py = fmaf(f, ey, py);
           pz = fmaf(f, ez, pz);
         } else {
-          const dvec4 M = nM[node];
-          const double dx = M.x - p0, dy = M.y - p1, dz = M.z - p2;
-          const double s = fma(dx, dx, fma(dy, dy, fma(dz, dz, eps2)));
-          if (!GUARD || s != 0.0) {
-            double y3;  // s^(-3/2) on the integer pipes, FP64 Newton steps outside its range
-            if (!emu::rsqrt_cube(s, y3)) {
-              const double y = rsqrt_f64(s);
-              y3 = y * (y * y);
-            }
-            const double f = M.w * y3;
-            ax = fma(f, dx, ax);
-            ay = fma(f, dy, ay);
-            az = fma(f, dz, az);
-          }
+          fq[(fq_head + fq_n) & (TW_FQ - 1)][threadIdx.x] = node;  // evaluated in a later round
+          fq_n++;
         }
         skip = nx;
         lane_next = nx;
       } else {
         lane_next = node + 1;
+      }
+    }
+    if (!MIXED) {
+      // a round of FP64 interactions when enough lanes have one waiting; a FIFO that
+      // just became full forces one, so a FIFO never holds more than TW_FQ
+      const unsigned waiting = __ballot_sync(0xffffffffu, fq_n > 0);
+      if (__popc(waiting) >= TW_FQ_ROUND || __any_sync(0xffffffffu, fq_n == TW_FQ)) {
+        if (fq_n > 0) {
+          const int c = fq[fq_head][threadIdx.x];
+          fq_head = (fq_head + 1) & (TW_FQ - 1);
+          fq_n--;
+          walk_interact_f64<GUARD>(nM, c, p0, p1, p2, eps2, ax, ay, az);
+        }
       }
     }
     // fold the FP32 partials every TW_FOLD warp steps (at most one interaction per
@@ -838,6 +868,14 @@ __global__ void __launch_bounds__(TW_THREADS, TW_MINB)
       pending = 0;
     }
     node = __reduce_min_sync(0xffffffffu, lane_next);
+  }
+  if (!MIXED) {
+    while (fq_n > 0) {  // the cells still waiting, in order
+      const int c = fq[fq_head][threadIdx.x];
+      fq_head = (fq_head + 1) & (TW_FQ - 1);
+      fq_n--;
+      walk_interact_f64<GUARD>(nM, c, p0, p1, p2, eps2, ax, ay, az);
+    }
   }
   if (STATS) {
     // one cell record read per warp step; the other counts summed over lanes
