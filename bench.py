@@ -63,7 +63,7 @@ def parse():
                          "over the ranks, positions all-gathered each step (strong scaling)")
     ap.add_argument("--cpu-targets", type=int, default=49152,
                     help="targets in the CPU-baseline sample (each against all N sources)")
-    ap.add_argument("--report", choices=["config0", "config1", "config2", "config3", "config4"],
+    ap.add_argument("--report", choices=["config0", "config1", "config2", "config3", "config4", "config4tangent"],
                     help="print one JSON line of the full measurements for that workload instead")
     return ap.parse_args()
 
@@ -185,7 +185,8 @@ def main():
         dev = torch.device("cuda", 0)
         torch.cuda.set_device(0)
         fn = {"config0": report_config0, "config1": report_config1, "config2": report_config2,
-              "config3": report_config3, "config4": report_config4}[args.report]
+              "config3": report_config3, "config4": report_config4,
+              "config4tangent": report_config4_tangent}[args.report]
         print(json.dumps({"report": args.report, **fn(dev)}), flush=True)
         return
     import numpy as np
@@ -773,6 +774,46 @@ def report_config4(dev, n=16384):
                                    "rel_err_per_coordinate": [float(f"{e:.3g}") for e in rel]}
         out[f"steps_{steps}"] = row
     return out
+
+
+def report_config4_tangent(dev, n=16384, steps=200, ncoord=64):
+    """Adjoint gradients with respect to x0 (FP64, checkpoints every 20) over the full
+    200-step rollout against exact directional derivatives of the same FP64 trajectory
+    from forward-mode tangent rollouts (``adjoint.tangent_rollout``), on the 64 random
+    coordinates of ``report_config4``; relative to the larger of |g_i| and 1e-3 max |g|."""
+    import numpy as np
+    import torch
+
+    from gravhopper_gb300 import engine, ics
+    from gravhopper_gb300.adjoint import rollout, tangent_rollout
+    ic = ics.plummer(n, seed=0)
+    x0 = torch.from_numpy(ic["pos"]).to(dev)
+    v0 = torch.from_numpy(ic["vel"]).to(dev)
+    m = torch.from_numpy(ic["mass"]).to(dev)
+    rng = np.random.default_rng(1)
+    xt = (x0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["pos"].shape)).to(dev)).contiguous()
+    vt = (v0 * torch.from_numpy(1 + 1e-3 * rng.normal(size=ic["vel"].shape)).to(dev)).contiguous()
+    engine.run_dkd(xt, vt, m, steps, 0.005, 5e-5, precision="fp64")
+    xa = x0.clone().requires_grad_(True)
+    xT, _ = rollout(xa, v0, m, steps, 0.005, 5e-5, checkpoint_every=20, precision="fp64")
+    ((xT - xt) ** 2).mean().backward()
+    g = xa.grad.reshape(-1)
+    idx = rng.choice(3 * n, size=ncoord, replace=False)
+    gmax = float(g.abs().max())
+    rel, same = [], True
+    t0 = time.perf_counter()
+    for i in idx:
+        u = torch.zeros(3 * n, dtype=torch.float64, device=dev)
+        u[int(i)] = 1.0
+        xT2, _, txT, _ = tangent_rollout(x0, v0, m, steps, 0.005, 5e-5, u.reshape(-1, 3), precision="fp64")
+        same = same and bool(torch.equal(xT2, xT.detach()))
+        d = float(2.0 * ((xT2 - xt) * txT).sum() / xt.numel())
+        gi = float(g[int(i)])
+        rel.append(abs(d - gi) / max(abs(gi), 1e-3 * gmax))
+    rel = np.array(rel)
+    return {"n": n, "steps": steps, "checkpoint_every": 20, "coordinates": ncoord,
+            "rel_err_max": float(rel.max()), "rel_err_median": float(np.median(rel)),
+            "final_state_bit_identical": same, "seconds": time.perf_counter() - t0}
 
 
 if __name__ == "__main__":

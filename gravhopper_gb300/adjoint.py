@@ -64,3 +64,39 @@ class _Rollout(torch.autograd.Function):
 def rollout(x0, v0, m, nsteps, dt, eps, checkpoint_every=20, precision="mixed"):
     """Differentiable ``nsteps`` leapfrog steps; returns (x_T, v_T)."""
     return _Rollout.apply(x0, v0, m, int(nsteps), float(dt), float(eps), int(checkpoint_every), precision)
+
+
+def tangent_rollout(x0, v0, m, nsteps, dt, eps, dx0, dv0=None, precision="fp64"):
+    """Forward-mode derivative of ``nsteps`` leapfrog steps along (dx0, dv0), masses
+    held fixed: returns (x_T, v_T, dx_T, dv_T).
+
+    The state advances by the engine's split step (first drift, direct-sum force, kick
+    and second drift; the fused step's operations, so the same bits as ``rollout``'s
+    forward pass), and the tangent by the same two linear step kernels with the
+    force's Jacobian-vector product J u = VJP(m u) / m: the direct sum's Jacobian
+    blocks are m_k M(x_k - x_i) (M the symmetric, even softened tidal tensor) and
+    -sum_j m_j M(x_j - x_i) on the diagonal, so the VJP kernel applied to the cotangent
+    m u gives m_i (J u)_i.  Every mass must be nonzero.  Costs one force and one VJP
+    per step; where ``rollout``'s adjoint gives the whole gradient of a scalar loss,
+    this gives the exact directional derivative of the same computed trajectory."""
+    md = m.detach().contiguous()
+    if bool((md == 0).any()):
+        raise ValueError("tangent_rollout: every mass must be nonzero")
+    x = x0.detach().clone().contiguous()
+    v = v0.detach().clone().contiguous()
+    tx = dx0.detach().clone().contiguous()
+    tv = torch.zeros_like(v) if dv0 is None else dv0.detach().clone().contiguous()
+    mm = md[:, None]
+    xh, txh, acc, cot, g, ta = (torch.empty_like(x) for _ in range(6))
+    gm = torch.empty_like(md)
+    for _ in range(int(nsteps)):
+        engine.dkd_drift(x, v, dt, out=xh)
+        engine.direct_force(xh, md, eps, precision=precision, out=acc)
+        engine.dkd_kick_drift(xh, v, acc, None, dt, out=x)
+        engine.dkd_drift(tx, tv, dt, out=txh)
+        torch.mul(txh, mm, out=cot)
+        engine.direct_vjp(xh, md, eps, cot, precision=precision, grad_pos=g, grad_mass=gm)
+        torch.div(g, mm, out=ta)
+        engine.dkd_kick_drift(txh, tv, ta, None, dt, out=tx)
+    return x, v, tx, tv
+
