@@ -315,7 +315,7 @@ def main():
 
     secondary, fp64 = {}, None
     if not args.no_secondary and rank == 0:
-        secondary = measure_secondary(ic, dev)
+        secondary = measure_secondary(ic, dev, fp64_peak)
         fp64 = measure_fp64(dev, fp64_peak)
 
     if rank == 0:
@@ -387,6 +387,8 @@ def tree_summary(tree):
     for key in ("theta_0.7", "theta_0.5"):
         t = tree.get(key, {})
         row = {p: float(f"{t[p]['particle_steps_per_s']:.4g}") for p in ("mixed", "fp64") if p in t}
+        if "fp64_pipe_frac" in t.get("fp64", {}):
+            row["fp64_walk_pipe_frac"] = float(f"{t['fp64']['fp64_pipe_frac']:.3g}")
         if "cpu_reference_s_per_step" in t:
             row["cpu_reference"] = float(f"{tree['n'] / t['cpu_reference_s_per_step']:.4g}")
             row["cpu_cores"] = t["cpu_reference_cores"]
@@ -394,7 +396,7 @@ def tree_summary(tree):
     return out
 
 
-def measure_secondary(ic, dev):
+def measure_secondary(ic, dev, fp64_peak=None):
     """Mixed-form accuracy, energy drift, tree, ensemble and adjoint on this GPU."""
     import numpy as np
     import torch
@@ -416,7 +418,7 @@ def measure_secondary(ic, dev):
     out["mixed_err_sample"] = f"{idx.numel()} targets of N={n} vs FP64 form"
     del x, m, a_mixed, a64
     out["energy_drift_10_steps"] = measure_energy_drift(dev)
-    out["tree"] = measure_tree(dev)
+    out["tree"] = measure_tree(dev, fp64_peak=fp64_peak)
     out["ensemble"] = measure_ensemble(dev)
     out["adjoint"] = measure_adjoint(dev)
     return out
@@ -450,8 +452,11 @@ def measure_energy_drift(dev, n=262144, steps=10):
     return out
 
 
-def measure_tree(dev, n=1 << 20, steps=2):
-    """Config 2: Hernquist + exponential disk, particle-steps/s of DKD steps with the tree."""
+def measure_tree(dev, n=1 << 20, steps=2, fp64_peak=None):
+    """Config 2: Hernquist + exponential disk, particle-steps/s of DKD steps with the tree.
+    For the FP64 walk also its FP64-pipe fraction: 10 FP64-pipe operations per
+    interaction (3 differences, 3 FMAs for r^2, one product, 3 accumulating FMAs) over
+    the timed walk, against the FP64 peak measured in the same process."""
     import numpy as np
     import torch
 
@@ -498,6 +503,8 @@ def measure_tree(dev, n=1 << 20, steps=2):
                               "record_read_gbs": rec_bytes / walk_s / 1e9,
                               "record_read_frac_of_measured_l2": rec_bytes / walk_s / l2,
                               "per_target_record_gbs": 48 * c["target_visits"] / walk_s / 1e9}
+            if prec == "fp64" and fp64_peak:
+                out[key][prec]["fp64_pipe_frac"] = 10.0 * c["interactions"] / walk_s / fp64_peak
     # CPU reference tree (the oracle restatement of _jbgrav.c) on a sample of targets:
     # its serial build plus the threaded walk of 16384 targets scaled to all N targets
     # (the faster of two calls).
