@@ -503,16 +503,19 @@ __device__ __forceinline__ int64_t cell_end(const uint64_t* __restrict__ keys, i
 // base[i] .. base[i] + d - lo in preorder.  nodes_kernel writes the leaf: the
 // particle's position as its centre, its mass, its skip index (gravoct_finalize,
 // _jbgrav.c:467-483: a leaf's centre of mass is its particle), and lists the
-// particles that open internal cells; nodes_internal_kernel gives those cells their
-// centre from the reference's FP64 recurrence along the particle's digits
-// (gravoct_add_particle, _jbgrav.c:403-428), their skip index and their monopole.  A
-// leaf is always accepted by the walk, so it needs no geometric centre.
+// particles that open internal cells and the internal cells themselves;
+// cell_centres_kernel gives those cells their centre from the reference's FP64
+// recurrence along the particle's digits (gravoct_add_particle, _jbgrav.c:403-428),
+// cells_kernel their skip index and their monopole.  A leaf is always accepted by the
+// walk, so it needs no geometric centre.
 __global__ void nodes_kernel(int64_t n, const int* __restrict__ lp, const int* __restrict__ depth,
                              const int* __restrict__ base, const uint32_t* __restrict__ perm,
                              const double* __restrict__ pos, const double* __restrict__ mass, NodeArrays na,
-                             int nnodes, int* __restrict__ list, int* __restrict__ count) {
+                             int nnodes, int* __restrict__ list, int* __restrict__ count,
+                             int2* __restrict__ cells, int* __restrict__ ncells) {
   const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   bool need = false;
+  int ncell = 0, k0 = 0;  // this particle's internal cells: nodes k0 .. k0 + ncell - 1
   if (i < n) {
     const int lo = lp[i] + 1, d = depth[i];
     const int k = base[i] + (d - lo);
@@ -526,21 +529,36 @@ __global__ void nodes_kernel(int64_t n, const int* __restrict__ lp, const int* _
     na.R[k].L = make_float4(f32_lo(x, hx), f32_lo(y, hy), f32_lo(z, hz), __int_as_float(next));
     na.R[k].O = make_float4(0.f, 0.f, 0.f, (float)m);
     need = d > lo;
+    ncell = d - lo;
+    k0 = base[i];
   }
   warp_append(need, i, list, count);
+  // the internal cells, one (cell, opener) entry each, for cells_kernel
+  const int lane = threadIdx.x & 31;
+  int incl = ncell;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  int first = 0;
+  if (lane == 31 && incl > 0) first = atomicAdd(ncells, incl);
+  first = __shfl_sync(0xffffffffu, first, 31) + incl - ncell;
+  for (int j = 0; j < ncell; j++) cells[first + j] = make_int2(k0 + j, (int)i);
 }
 
 __device__ __forceinline__ double rcp_f64(double m);
 
-__global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
-                                      const int* __restrict__ lp, const int* __restrict__ depth,
-                                      const int* __restrict__ base, const TreeRoot* __restrict__ root,
-                                      NodeArrays na, int nnodes, const int* __restrict__ list,
-                                      const int* __restrict__ count, const FxMoments* __restrict__ fx_local,
-                                      const FxMoments* __restrict__ fx_tiles) {
+// Centres of the internal cells from the reference's FP64 recurrence along each
+// opener's digits (gravoct_add_particle, _jbgrav.c:403-428): C[k] = (centre, size).
+// Only the recurrence runs here, so its FP64 adds keep most lanes of a warp busy; the
+// rest of each cell is cells_kernel's, one thread per cell.
+__global__ void cell_centres_kernel(const uint64_t* __restrict__ keys, int words, int64_t n,
+                                    const int* __restrict__ lp, const int* __restrict__ depth,
+                                    const int* __restrict__ base, const TreeRoot* __restrict__ root, NodeArrays na,
+                                    const int* __restrict__ list, const int* __restrict__ count) {
   __shared__ double offs[TREE_MAX_LEVELS];  // size 2^-(L+2), exact
   const double S = root->size;
-  const int lsb_m = root->lsb_m, lsb_f = root->lsb_f;
   for (int l = threadIdx.x; l < TREE_MAX_LEVELS; l += blockDim.x)
     offs[l] = dmul(S, __longlong_as_double((long long)(1023 - (l + 2)) << 52));
   __syncthreads();
@@ -549,39 +567,11 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
     const int64_t i = list[q];
     const int lo = lp[i] + 1, d = depth[i];
     const int k0 = base[i];
-    const FxMoments Pi = fxm_prefix(fx_local, fx_tiles, i, n);  // every cell i opens starts at i
     const uint64_t kw0 = keys[i], kw1 = words > 1 ? keys[n + i] : 0ull;  // digits of the first 42 levels
     double c[3] = {root->c[0], root->c[1], root->c[2]};
     for (int L = 0; L < d; L++) {
-      if (L >= lo) {
-        const int k = k0 + (L - lo);
-        const int64_t end = cell_end(keys, words, n, lp, i, L);
-        const int next = end < n ? base[end] : nnodes;
-        const double size = dmul(S, __longlong_as_double((long long)(1023 - L) << 52));
-        float4 A, Lo;
-        A.x = f32_hi(c[0]);
-        A.y = f32_hi(c[1]);
-        A.z = f32_hi(c[2]);
-        A.w = (float)dmul(size, size);
-        Lo.x = f32_lo(c[0], A.x);
-        Lo.y = f32_lo(c[1], A.y);
-        Lo.z = f32_lo(c[2], A.z);
-        Lo.w = __int_as_float(next);
-        na.R[k].A = A;
-        na.R[k].L = Lo;
-        na.C[k] = make_dvec4(c[0], c[1], c[2], size);
-        // monopole of particles [i, end): exact sums, one rounding each, then
-        // firstmoment / mass (_jbgrav.c:478) with a Newton-refined reciprocal
-        const FxMoments Pe = fxm_prefix(fx_local, fx_tiles, end, n);
-        const double cm = fx::to_double(fx::sub(Pe.c[0], Pi.c[0]), lsb_m);
-        const double r = rcp_f64(cm);
-        double com[3];
-#pragma unroll
-        for (int a = 0; a < 3; a++) com[a] = dmul(fx::to_double(fx::sub(Pe.c[a + 1], Pi.c[a + 1]), lsb_f), r);
-        na.M[k] = make_dvec4(com[0], com[1], com[2], cm);
-        na.R[k].O = make_float4((float)dsub(com[0], c[0]), (float)dsub(com[1], c[1]), (float)dsub(com[2], c[2]),
-                                (float)cm);
-      }
+      if (L >= lo)
+        na.C[k0 + (L - lo)] = make_dvec4(c[0], c[1], c[2], dmul(S, __longlong_as_double((long long)(1023 - L) << 52)));
       if (L + 1 < d) {
         const unsigned g = L < KEY_LEVELS       ? (unsigned)(kw0 >> (3 * (KEY_LEVELS - 1 - L))) & 7u
                            : L < 2 * KEY_LEVELS ? (unsigned)(kw1 >> (3 * (2 * KEY_LEVELS - 1 - L))) & 7u
@@ -592,6 +582,49 @@ __global__ void nodes_internal_kernel(const uint64_t* __restrict__ keys, int wor
       }
     }
   }
+}
+
+// One internal cell per thread (the (cell, opener) list of nodes_kernel): its skip
+// index, its walk record from the centre, and its monopole.  Cell k of opener i is at
+// level L = lp[i] + 1 + (k - base[i]) and holds the key-ordered particles [i, end).
+__global__ void cells_kernel(const uint64_t* __restrict__ keys, int words, int64_t n, const int* __restrict__ lp,
+                             const int* __restrict__ base, const TreeRoot* __restrict__ root, NodeArrays na,
+                             int nnodes, const int2* __restrict__ cells, int ncells,
+                             const FxMoments* __restrict__ fx_local, const FxMoments* __restrict__ fx_tiles) {
+  const int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= ncells) return;
+  const int2 e = cells[q];
+  const int k = e.x;
+  const int64_t i = e.y;
+  const int L = lp[i] + 1 + (k - base[i]);
+  const int lsb_m = root->lsb_m, lsb_f = root->lsb_f;
+  const dvec4 C = na.C[k];
+  const int64_t end = cell_end(keys, words, n, lp, i, L);
+  const int next = end < n ? base[end] : nnodes;
+  const double c[3] = {C.x, C.y, C.z};
+  float4 A, Lo;
+  A.x = f32_hi(c[0]);
+  A.y = f32_hi(c[1]);
+  A.z = f32_hi(c[2]);
+  A.w = (float)dmul(C.w, C.w);
+  Lo.x = f32_lo(c[0], A.x);
+  Lo.y = f32_lo(c[1], A.y);
+  Lo.z = f32_lo(c[2], A.z);
+  Lo.w = __int_as_float(next);
+  na.R[k].A = A;
+  na.R[k].L = Lo;
+  // monopole of particles [i, end): exact sums, one rounding each, then
+  // firstmoment / mass (_jbgrav.c:478) with a Newton-refined reciprocal
+  const FxMoments Pi = fxm_prefix(fx_local, fx_tiles, i, n);
+  const FxMoments Pe = fxm_prefix(fx_local, fx_tiles, end, n);
+  const double cm = fx::to_double(fx::sub(Pe.c[0], Pi.c[0]), lsb_m);
+  const double r = rcp_f64(cm);
+  double com[3];
+#pragma unroll
+  for (int a2 = 0; a2 < 3; a2++) com[a2] = dmul(fx::to_double(fx::sub(Pe.c[a2 + 1], Pi.c[a2 + 1]), lsb_f), r);
+  na.M[k] = make_dvec4(com[0], com[1], com[2], cm);
+  na.R[k].O = make_float4((float)dsub(com[0], c[0]), (float)dsub(com[1], c[1]), (float)dsub(com[2], c[2]),
+                          (float)cm);
 }
 
 // ---------------------------------------------------------------------------
@@ -908,6 +941,7 @@ struct TreeWS {
   Buffer nA, nC, nM, fxl, fxt, xh[2];
   Buffer tkeys, tkeys_tmp, tidx, tidx_tmp, trs;  // target points' walk order
   Buffer list;                // particle lists: key fallbacks, then cell openers
+  Buffer cells;               // (internal cell, opener) pairs
   int* host_flags = nullptr;  // pinned: the 8 device flags, nnodes, the root's non-finite flag
   int words = TREE_MIN_WORDS;
   int64_t full_sort_n = -1;  // particle count whose last build needed the full multi-word sort
@@ -960,7 +994,7 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   GH_TRY(ensure(ws.base, (n + 1) * sizeof(int)));
   GH_TRY(ensure(ws.scan, scan_scratch_ints(n) * sizeof(int)));
   // flags: [0] full-key tie, [1] deepest level, [2] long run, [3] key fallbacks, [4] cell openers,
-  // [5] a bounded wait in the sort gave up
+  // [5] a bounded wait in the sort gave up, [6] internal cells listed
   GH_TRY(ensure(ws.flags, 8 * sizeof(int)));
   GH_TRY(ensure(ws.list, n * sizeof(int)));
   GH_TRY(ensure(ws.idx, n * sizeof(uint32_t)));
@@ -1053,6 +1087,9 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
   const int64_t ntiles = (n + MS_TILE - 1) / MS_TILE;
   GH_TRY(ensure(ws.fxl, (size_t)n * sizeof(FxMoments)));
   GH_TRY(ensure(ws.fxt, (size_t)(ntiles + 1) * sizeof(FxMoments)));
+  // every node that is not a particle's leaf is an internal cell
+  const int64_t ncells = (int64_t)nnodes - n;
+  GH_TRY(ensure(ws.cells, (size_t)(ncells > 0 ? ncells : 1) * sizeof(int2)));
   NodeArrays na = node_arrays(ws);
   {
     const uint64_t* keys = (const uint64_t*)ws.keys.ptr;
@@ -1068,12 +1105,19 @@ static int tree_build(TreeWS& ws, const double* pos, const double* mass, int64_t
     GH_LAUNCH_CHECK();
     moments_tiles_kernel<<<1, MS_THREADS, 0, st>>>(fxt, ntiles);
     GH_LAUNCH_CHECK();
-    // 4. leaves, then internal cells with their centres and monopoles
-    nodes_kernel<<<gn, T, 0, st>>>(n, lp, dep, bs, perm, pos, mass, na, nnodes, (int*)ws.list.ptr, openers);
+    // 4. leaves, then the internal cells' centres, then the rest of each internal cell
+    int2* cells = (int2*)ws.cells.ptr;
+    nodes_kernel<<<gn, T, 0, st>>>(n, lp, dep, bs, perm, pos, mass, na, nnodes, (int*)ws.list.ptr, openers, cells,
+                                   (int*)ws.flags.ptr + 6);
     GH_LAUNCH_CHECK();
-    nodes_internal_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(keys, words, n, lp, dep, bs, root, na, nnodes,
-                                                                    (const int*)ws.list.ptr, openers, fxl, fxt);
+    cell_centres_kernel<<<gn < 4 * 152 ? gn : 4 * 152, T, 0, st>>>(keys, words, n, lp, dep, bs, root, na,
+                                                                  (const int*)ws.list.ptr, openers);
     GH_LAUNCH_CHECK();
+    if (ncells > 0) {
+      cells_kernel<<<(unsigned)((ncells + T - 1) / T), T, 0, st>>>(keys, words, n, lp, bs, root, na, nnodes, cells,
+                                                                   (int)ncells, fxl, fxt);
+      GH_LAUNCH_CHECK();
+    }
   }
   out->nnodes = nnodes;
   out->maxdepth = maxdepth;
