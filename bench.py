@@ -46,6 +46,7 @@ sys.path.insert(0, ROOT)
 METRIC = "Direct-sum Gpair/s & tree particle-steps/s, mixed vs FP64, 1 GB300 @ <=1e-6 err"
 UNIT = "Gpair/s"
 PAIR_OPS = 12  # FP32 FMA-pipe lane-ops per pair: 3 sub, 3 fma, 3 mul, 3 fma
+PAIR_OPS_EQ = 11  # the same with equal masses: the mass is applied once per target
 PAIR_OPS_FP64 = 12  # FP64-pipe ops per pair of the FP64 form: 3 sub, 6 mul, 3 add
 
 
@@ -210,7 +211,11 @@ def main():
     eps, dt = 5e-5, 0.005
     stream = torch.cuda.current_stream()
     fp32_peak, fp64_peak = _capi.measure_fma_peaks()
-    mix_ceiling = _capi.measure_pair_mix()  # the pair's instruction mix with operands in registers
+    # equal masses (as the Plummer spheres here) run the kernel's equal-mass loop
+    equal_mass = bool(np.all(ic["mass"] == ic["mass"][0]) and ic["mass"][0] != 0)
+    pair_ops = PAIR_OPS_EQ if equal_mass else PAIR_OPS
+    # the pair's instruction mix with operands in registers
+    mix_ceiling = _capi.measure_pair_mix(equal_mass=equal_mass)
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     def barrier():
@@ -290,10 +295,10 @@ def main():
     # pairs one force launch evaluates (sharded: this rank's targets, own and others' sources)
     achieved = (pairs if not shard else float(x.shape[0]) * n * args.steps / max(kern_n, 1)) / kern_avg_s / 1e9
     mixed = args.precision == "mixed"
-    # mixed: 12 FP32 FMA-pipe lane-ops per pair; FP64: the 12 of the reference's pair
-    # operations that stay on the FP64 pipe (squared distance, division and square
-    # root run as exact integer arithmetic)
-    peak = (fp32_peak if mixed else fp64_peak) / (PAIR_OPS if mixed else PAIR_OPS_FP64) / 1e9
+    # mixed: 12 FP32 FMA-pipe lane-ops per pair (11 with equal masses); FP64: the 12 of
+    # the reference's pair operations that stay on the FP64 pipe (squared distance,
+    # division and square root run as exact integer arithmetic)
+    peak = (fp32_peak if mixed else fp64_peak) / (pair_ops if mixed else PAIR_OPS_FP64) / 1e9
     # DRAM bytes (read + write) of one launch of the fused DKD kernel at N = 1,048,576,
     # from one single-pass ncu capture (dram__bytes_read.sum 78.47 MB + write 29.32 MB;
     # profiles/direct_mixed_bench_n1048576_launches.md); other sizes: not captured
@@ -303,13 +308,16 @@ def main():
                 "achieved": achieved, "peak": peak, "unit": UNIT,
                 "frac": achieved / peak, "traffic": traffic,
                 "peak_source": (f"measured live: f32x2 FMA chains, {fp32_peak / 1e12:.1f} T lane-op/s "
-                                f"/ {PAIR_OPS} lane-ops per pair") if mixed else
+                                f"/ {pair_ops} lane-ops per pair"
+                                + (" (equal masses: no per-pair mass multiply)" if equal_mass else ""))
+                               if mixed else
                                (f"measured live: FP64 FMA chains, {fp64_peak / 1e12:.2f} T lane-op/s "
                                 f"/ {PAIR_OPS_FP64} FP64-pipe ops per pair"),
                 "tflops_20_per_pair": achieved * 20 / 1e3, "kernel_launches_timed": kern_n}
     if mixed:
-        # what the same 12 FMA-pipe instructions and one MUFU per pair reach with every
-        # operand in registers (gh_measure_pair_mix): the mix's own ceiling
+        # what the same FMA-pipe instructions (12, or 11 with equal masses) and one MUFU
+        # per pair reach with every operand in registers (gh_measure_pair_mix): the
+        # mix's own ceiling
         roofline["mix_ceiling"] = {"value": mix_ceiling / 1e9, "unit": UNIT, "frac": achieved / (mix_ceiling / 1e9),
                                    "of_fma_peak": mix_ceiling / 1e9 / peak}
 

@@ -92,7 +92,7 @@ SIGNATURES = {
     "gh_kernel_timing": (_int, [_int]),
     "gh_kernel_timing_collect": (_int, [_vp, _vp]),
     "gh_measure_l2_read": (_int, [_vp, _vp]),
-    "gh_measure_pair_mix": (_int, [_vp, _vp]),
+    "gh_measure_pair_mix": (_int, [_int, _vp, _vp]),
     "gh_check_inv_cube": (_int, [_i64, _u64, _vp, _vp]),
     "gh_tree_stats": (_int, [_int]),
     "gh_tree_stats_read": (_int, [_vp]),
@@ -178,11 +178,12 @@ def kernel_timing_collect():
     return ms.value, n.value
 
 
-def measure_pair_mix(stream=None):
+def measure_pair_mix(equal_mass=False, stream=None):
     """Pairs per second of the mixed direct sum's pair arithmetic with operands in
-    registers on the current device (the instruction mix's ceiling)."""
+    registers on the current device (the instruction mix's ceiling); ``equal_mass``:
+    the loop that systems of equal masses run (no per-pair mass multiply)."""
     p = ctypes.c_double(0.0)
-    call("gh_measure_pair_mix", ctypes.addressof(p), stream_handle(stream))
+    call("gh_measure_pair_mix", 1 if equal_mass else 0, ctypes.addressof(p), stream_handle(stream))
     return p.value
 
 

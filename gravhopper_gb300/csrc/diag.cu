@@ -194,11 +194,13 @@ __global__ void __launch_bounds__(256)
 
 // The mixed direct sum's pair arithmetic with every operand in registers: per pair 3
 // subtractions, 3 FMAs for r^2 + eps^2, one MUFU rsqrt, 3 multiplies and 3 FMAs into
-// the accumulators (12 FMA-pipe instructions and one MUFU), MIX_R targets per thread,
-// the "source" rotated through registers; no memory in the loop.  Its pairs per second
-// are the ceiling that mix reaches on this GPU, below the pure FMA-chain peak.
+// the accumulators (12 FMA-pipe instructions and one MUFU; EQ, the equal-mass loop: 2
+// multiplies, 11 instructions), MIX_R targets per thread, the "source" rotated through
+// registers; no memory in the loop.  Its pairs per second are the ceiling that mix
+// reaches on this GPU, below the pure FMA-chain peak.
 constexpr int MIX_THREADS = 512, MIX_R = 4, MIX_UNROLL = 4;
 
+template <bool EQ>
 __global__ void __launch_bounds__(MIX_THREADS, 1) pair_mix_kernel(int iters, float seed, float* out) {
   float sx[MIX_R], sy[MIX_R], sz[MIX_R], ax[MIX_R], ay[MIX_R], az[MIX_R];
 #pragma unroll
@@ -218,7 +220,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 1) pair_mix_kernel(int iters, flo
         const float dx = a.x - sx[r], dy = a.y - sy[r], dz = a.z - sz[r];
         const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, e2)));
         const float ri = rsqrt_approx(r2);
-        const float sc = (a.w * ri) * (ri * ri);
+        const float sc = EQ ? ri * (ri * ri) : (a.w * ri) * (ri * ri);
         ax[r] = fmaf(sc, dx, ax[r]);
         ay[r] = fmaf(sc, dy, ay[r]);
         az[r] = fmaf(sc, dz, az[r]);
@@ -234,7 +236,7 @@ __global__ void __launch_bounds__(MIX_THREADS, 1) pair_mix_kernel(int iters, flo
 
 }  // namespace gh
 
-extern "C" int gh_measure_pair_mix(double* pairs_per_s, void* stream) {
+extern "C" int gh_measure_pair_mix(int equal_mass, double* pairs_per_s, void* stream) {
   using namespace gh;
   clear_error();
   if (!pairs_per_s) return set_error(GH_ERR_ARG, "pair mix: null output");
@@ -250,7 +252,10 @@ extern "C" int gh_measure_pair_mix(double* pairs_per_s, void* stream) {
   float best = 1e30f;
   for (int rep = 0; rep < 3; rep++) {
     GH_CUDA_TRY(cudaEventRecord(e0, st));
-    pair_mix_kernel<<<blocks, MIX_THREADS, 0, st>>>(iters, 1e-3f, (float*)sink.ptr);
+    if (equal_mass)
+      pair_mix_kernel<true><<<blocks, MIX_THREADS, 0, st>>>(iters, 1e-3f, (float*)sink.ptr);
+    else
+      pair_mix_kernel<false><<<blocks, MIX_THREADS, 0, st>>>(iters, 1e-3f, (float*)sink.ptr);
     GH_LAUNCH_CHECK();
     GH_CUDA_TRY(cudaEventRecord(e1, st));
     GH_CUDA_TRY(cudaEventSynchronize(e1));

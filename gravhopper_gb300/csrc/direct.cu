@@ -14,20 +14,27 @@ namespace gh {
 constexpr int COM_THREADS = 256;
 constexpr int COM_MAX_BLOCKS = 512;
 
+// Also flags, per block, whether every mass of the block equals mass[0] (a NaN never
+// does), for the mixed kernel's equal-mass loop.
 __global__ void com_partial_kernel(const double* __restrict__ pos, const double* __restrict__ mass,
-                                   int64_t n, dvec4* __restrict__ part) {
+                                   int64_t n, dvec4* __restrict__ part, int* __restrict__ differ) {
   __shared__ dvec4 red[COM_THREADS];
   const int64_t per = (n + gridDim.x - 1) / gridDim.x;
   const int64_t b0 = (int64_t)blockIdx.x * per;
   const int64_t b1 = b0 + per < n ? b0 + per : n;
+  const double m0 = n > 0 ? mass[0] : 0.0;
   dvec4 acc = make_dvec4(0.0, 0.0, 0.0, 0.0);
+  bool ne = false;
   for (int64_t i = b0 + threadIdx.x; i < b1; i += COM_THREADS) {
     double m = mass[i];
+    ne |= !(m == m0);
     acc.x += m * pos[3 * i];
     acc.y += m * pos[3 * i + 1];
     acc.z += m * pos[3 * i + 2];
     acc.w += m;
   }
+  ne = __syncthreads_or(ne);
+  if (threadIdx.x == 0) differ[blockIdx.x] = ne;
   red[threadIdx.x] = acc;
   __syncthreads();
   for (int s = COM_THREADS / 2; s > 0; s >>= 1) {
@@ -43,15 +50,22 @@ __global__ void com_partial_kernel(const double* __restrict__ pos, const double*
   if (threadIdx.x == 0) part[blockIdx.x] = red[0];
 }
 
-__global__ void com_final_kernel(const dvec4* __restrict__ part, int nb, double* __restrict__ origin) {
+// origin[0..2]: the mass-weighted centre; origin[3]: the common mass of all particles
+// when they share one that is finite and nonzero, else 0.
+__global__ void com_final_kernel(const dvec4* __restrict__ part, const int* __restrict__ differ, int nb,
+                                 const double* __restrict__ mass, int64_t n, double* __restrict__ origin) {
   if (threadIdx.x != 0 || blockIdx.x != 0) return;
   dvec4 s = make_dvec4(0.0, 0.0, 0.0, 0.0);
+  bool ne = false;
   for (int b = 0; b < nb; b++) {
     s.x += part[b].x;
     s.y += part[b].y;
     s.z += part[b].z;
     s.w += part[b].w;
+    ne |= differ[b] != 0;
   }
+  const double m0 = n > 0 ? mass[0] : 0.0;
+  origin[3] = (!ne && m0 != 0.0 && isfinite(m0)) ? m0 : 0.0;
   if (s.w != 0.0 && isfinite(s.x / s.w) && isfinite(s.y / s.w) && isfinite(s.z / s.w)) {
     origin[0] = s.x / s.w;
     origin[1] = s.y / s.w;
@@ -146,9 +160,10 @@ static int auto_shape(int64_t np, int64_t nt, bool dkd) {
 
 template <bool G, int T, int P, int B, class Epi, bool PK = true>
 static int launch_shape(const StreamK& sk, const float4* src, int64_t np, const float4* tgt, int64_t nt,
-                        float eps2, float* partials, int* counters, const Epi& epi, cudaStream_t st) {
+                        float eps2, float* partials, int* counters, const Epi& epi, const double* eqm,
+                        cudaStream_t st) {
   direct_mixed_kernel<G, T, P, B, Epi, PK><<<(unsigned)sk.grid, T, 0, st>>>(src, np, tgt, nt, eps2, sk, partials,
-                                                                            counters, epi);
+                                                                            counters, epi, eqm);
   return GH_OK;
 }
 
@@ -165,21 +180,21 @@ static int occupancy_shape() {
 template <bool G, class Epi>
 static int dispatch_shape(int shape, const StreamK& sk, const float4* src, int64_t np, const float4* tgt,
                           int64_t nt, float eps2, float* partials, int* counters, const Epi& epi,
-                          cudaStream_t st) {
+                          const double* eqm, cudaStream_t st) {
   switch (shape) {
-    case 0: return launch_shape<G, 256, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 1: return launch_shape<G, 256, 4, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 2: return launch_shape<G, 128, 4, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 3: return launch_shape<G, 128, 2, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 4: return launch_shape<G, 512, 2, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 5: return launch_shape<G, 256, 2, 3>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 6: return launch_shape<G, 128, 2, 6>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 7: return launch_shape<G, 256, 1, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 8: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 9: return launch_shape<G, 256, 2, 2, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 10: return launch_shape<G, 512, 2, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    case 11: return launch_shape<G, 256, 4, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
-    default: return launch_shape<G, 384, 3, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    case 0: return launch_shape<G, 256, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 1: return launch_shape<G, 256, 4, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 2: return launch_shape<G, 128, 4, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 3: return launch_shape<G, 128, 2, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 4: return launch_shape<G, 512, 2, 1>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 5: return launch_shape<G, 256, 2, 3>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 6: return launch_shape<G, 128, 2, 6>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 7: return launch_shape<G, 256, 1, 4>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 8: return launch_shape<G, 512, 2, 2>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 9: return launch_shape<G, 256, 2, 2, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 10: return launch_shape<G, 512, 2, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    case 11: return launch_shape<G, 256, 4, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
+    default: return launch_shape<G, 384, 3, 1, Epi, false>(sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
   }
 }
 
@@ -260,17 +275,20 @@ int set_mixed_shape(int shape) {
   return GH_OK;
 }
 
-// Mass-weighted centre of (pos, mass) into ws.origin (3 doubles).
+// Mass-weighted centre of (pos, mass) into ws.origin[0..2], and the particles' common
+// mass (0 when they differ) into ws.origin[3].
 static int compute_origin(DirectWS& ws, const double* pos, const double* mass, int64_t n,
                           cudaStream_t st) {
   GH_TRY(ensure(ws.origin, 4 * sizeof(double)));
-  GH_TRY(ensure(ws.com_part, COM_MAX_BLOCKS * sizeof(dvec4)));
+  GH_TRY(ensure(ws.com_part, COM_MAX_BLOCKS * (sizeof(dvec4) + sizeof(int))));
   int nb = (int)((n + 4 * COM_THREADS - 1) / (4 * COM_THREADS));
   if (nb < 1) nb = 1;
   if (nb > COM_MAX_BLOCKS) nb = COM_MAX_BLOCKS;
-  com_partial_kernel<<<nb, COM_THREADS, 0, st>>>(pos, mass, n, (dvec4*)ws.com_part.ptr);
+  dvec4* part = (dvec4*)ws.com_part.ptr;
+  int* differ = (int*)(part + COM_MAX_BLOCKS);
+  com_partial_kernel<<<nb, COM_THREADS, 0, st>>>(pos, mass, n, part, differ);
   GH_LAUNCH_CHECK();
-  com_final_kernel<<<1, 32, 0, st>>>((const dvec4*)ws.com_part.ptr, nb, (double*)ws.origin.ptr);
+  com_final_kernel<<<1, 32, 0, st>>>(part, differ, nb, mass, n, (double*)ws.origin.ptr);
   GH_LAUNCH_CHECK();
   return GH_OK;
 }
@@ -302,10 +320,12 @@ static int launch_mixed(DirectWS& ws, const float4* src, int64_t np, const float
   float* partials = (float*)ws.partials.ptr;
   int* counters = (int*)ws.counters.ptr;
   prof_begin(st);
+  // the sources' common mass, when they share one (compute_origin), else 0
+  const double* eqm = (const double*)ws.origin.ptr + 3;
   if (guard)
-    dispatch_shape<true>(shape, sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    dispatch_shape<true>(shape, sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
   else
-    dispatch_shape<false>(shape, sk, src, np, tgt, nt, eps2, partials, counters, epi, st);
+    dispatch_shape<false>(shape, sk, src, np, tgt, nt, eps2, partials, counters, epi, eqm, st);
   prof_end(st);
   GH_LAUNCH_CHECK();
   return GH_OK;

@@ -327,8 +327,10 @@ __host__ __device__ __forceinline__ int64_t sk_owner(const StreamK& s, int64_t u
 // One shared-memory chunk of JT sources against P packed target pairs: FP32 pair
 // forces summed into a per-chunk partial, then folded into the (h, l) two-sum
 // accumulator.  `tile` holds each source duplicated per lane: (x,x,y,y), (z,z,m,m).
-// Per pair: 3 sub, 3 fma (r^2 + eps^2), 1 MUFU rsqrt, 3 mul, 3 fma.
-template <bool GUARD, int P, int JT>
+// Per pair: 3 sub, 3 fma (r^2 + eps^2), 1 MUFU rsqrt, 3 mul, 3 fma.  EQ (all sources
+// of one mass): the sum of r^-3 d without the mass, which the caller applies once per
+// target; 2 multiplies per pair instead of 3.
+template <bool GUARD, int P, int JT, bool EQ = false>
 __device__ __forceinline__ void mixed_chunk(const float4* __restrict__ tile, const f2* tx, const f2* ty,
                                             const f2* tz, f2 E2, f2* hx, f2* hy, f2* hz, f2* lx, f2* ly,
                                             f2* lz) {
@@ -358,8 +360,7 @@ __device__ __forceinline__ void mixed_chunk(const float4* __restrict__ tile, con
       }
       f2 ri = f2make(ia, ib);
       f2 ri2 = f2mul(ri, ri);
-      f2 mri = f2mul(M, ri);
-      f2 sc = f2mul(mri, ri2);
+      f2 sc = EQ ? f2mul(ri, ri2) : f2mul(f2mul(M, ri), ri2);
       px[p] = f2fma(sc, dx, px[p]);
       py[p] = f2fma(sc, dy, py[p]);
       pz[p] = f2fma(sc, dz, pz[p]);
@@ -382,7 +383,7 @@ __device__ __forceinline__ void mixed_chunk(const float4* __restrict__ tile, con
 
 // The same chunk with scalar FP32 instructions (one target per instruction); its
 // sources are stored once each, (x, y, z, m), not duplicated per lane pair.
-template <bool GUARD, int P, int JT>
+template <bool GUARD, int P, int JT, bool EQ = false>
 __device__ __forceinline__ void mixed_chunk_scalar(const float4* __restrict__ tile, const f2* tx, const f2* ty,
                                                    const f2* tz, f2 E2, f2* hx, f2* hy, f2* hz, f2* lx, f2* ly,
                                                    f2* lz) {
@@ -407,7 +408,7 @@ __device__ __forceinline__ void mixed_chunk_scalar(const float4* __restrict__ ti
       const float r2 = fmaf(dz, dz, fmaf(dy, dy, fmaf(dx, dx, e2)));
       float ri = rsqrt_approx(r2);
       if (GUARD) ri = r2 > 0.f ? ri : 0.f;
-      const float sc = (a.w * ri) * (ri * ri);
+      const float sc = EQ ? ri * (ri * ri) : (a.w * ri) * (ri * ri);
       ax[r] = fmaf(sc, dx, ax[r]);
       ay[r] = fmaf(sc, dy, ay[r]);
       az[r] = fmaf(sc, dz, az[r]);
@@ -438,7 +439,7 @@ template <bool GUARD, int THREADS, int P, int MINB, class Epi, bool PACKED = tru
 __global__ void __launch_bounds__(THREADS, MINB)
     direct_mixed_kernel(const float4* __restrict__ src, int64_t np, const float4* __restrict__ tgt,
                         int64_t nt, float eps2, StreamK sk, float* __restrict__ partials,
-                        int* __restrict__ counters, Epi epi) {
+                        int* __restrict__ counters, Epi epi, const double* __restrict__ eqm) {
   constexpr int R = 2 * P, TILE = THREADS * R, JT = THREADS;
   constexpr int64_t SLOT = mixed_slot_floats(THREADS, P);
   // Sources duplicated per lane pair: (x,x,y,y) and (z,z,m,m).
@@ -449,6 +450,11 @@ __global__ void __launch_bounds__(THREADS, MINB)
   const int64_t g = blockIdx.x;
   const int64_t u_begin = sk_start(sk, g), u_end = sk_start(sk, g + 1);
   const f2 E2 = f2make(eps2, eps2);
+  // *eqm: the sources' common mass when every source has it (0: masses differ, or no
+  // pointer); then the chunks sum r^-3 d and each target's sum is scaled by it once
+  const double mq = eqm ? __ldg(eqm) : 0.0;
+  const bool eq = mq != 0.0;
+  const double msc = eq ? mq : 1.0;  // x * 1.0 == x: the general path's bits are unchanged
 
   int64_t u = u_begin;
   while (u < u_end) {
@@ -479,10 +485,15 @@ __global__ void __launch_bounds__(THREADS, MINB)
     // barrier per chunk suffices (the barrier of chunk c orders every read of the
     // buffer it reuses, last read in chunk c-1).  Padding sources have zero mass at the
     // origin: their terms are exactly 0.
+    // With equal masses (eq) a staged source's w is 1 (0 for padding past the last
+    // source) instead of its mass: the equal-mass loop, which ignores w, runs only on
+    // full chunks, and the general loop on the partial last chunk then gives r^-3 d
+    // for a source and exactly 0 for padding.
     float4 pre;
     {
       const int64_t j = c0 * JT + tid;
       pre = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (eq) pre.w = j < np ? 1.f : 0.f;
     }
     for (int64_t c = c0; c < c1; c++) {
       float4* tb = tile + buf * (2 * JT);
@@ -496,11 +507,20 @@ __global__ void __launch_bounds__(THREADS, MINB)
       if (c + 1 < c1) {
         const int64_t j = (c + 1) * JT + tid;
         pre = j < np ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (eq) pre.w = j < np ? 1.f : 0.f;
       }
-      if (PACKED)
-        mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
-      else
-        mixed_chunk_scalar<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      const bool eq_loop = eq && (c + 1) * JT <= np;  // a full chunk of equal masses
+      if (PACKED) {
+        if (eq_loop)
+          mixed_chunk<GUARD, P, JT, true>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+        else
+          mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      } else {
+        if (eq_loop)
+          mixed_chunk_scalar<GUARD, P, JT, true>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+        else
+          mixed_chunk_scalar<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      }
       buf ^= 1;
     }
 
@@ -518,11 +538,11 @@ __global__ void __launch_bounds__(THREADS, MINB)
         int64_t i0 = t * TILE + (2 * p) * THREADS + tid;
         int64_t i1 = i0 + THREADS;
         if (i0 < nt)
-          epi(i0, (double)a[0] + (double)a[1], (double)a[2] + (double)a[3],
-              (double)a[4] + (double)a[5]);
+          epi(i0, msc * ((double)a[0] + (double)a[1]), msc * ((double)a[2] + (double)a[3]),
+              msc * ((double)a[4] + (double)a[5]));
         if (i1 < nt)
-          epi(i1, (double)b[0] + (double)b[1], (double)b[2] + (double)b[3],
-              (double)b[4] + (double)b[5]);
+          epi(i1, msc * ((double)b[0] + (double)b[1]), msc * ((double)b[2] + (double)b[3]),
+              msc * ((double)b[4] + (double)b[5]));
       }
       continue;
     }
@@ -575,8 +595,8 @@ __global__ void __launch_bounds__(THREADS, MINB)
         }
       }
       if (i < nt)
-        epi(i, (double)h[0] + (double)l[0], (double)h[1] + (double)l[1],
-            (double)h[2] + (double)l[2]);
+        epi(i, msc * ((double)h[0] + (double)l[0]), msc * ((double)h[1] + (double)l[1]),
+            msc * ((double)h[2] + (double)l[2]));
     }
     if (tid == 0) counters[t] = 0;  // ready for the next launch
   }

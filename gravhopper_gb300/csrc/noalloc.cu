@@ -153,10 +153,12 @@ extern "C" int gh_direct_mixed_noalloc(const double* pos, const double* mass, in
   EpiStore epi{acc};
   if (guard)
     direct_mixed_kernel<true, NA_THREADS, NA_P, NA_MINB, EpiStore>
-        <<<(unsigned)sk.grid, NA_THREADS, 0, st>>>(src, np, src, np, eps2, sk, partials, counters, epi);
+        <<<(unsigned)sk.grid, NA_THREADS, 0, st>>>(src, np, src, np, eps2, sk, partials, counters, epi,
+                                                   nullptr);
   else
     direct_mixed_kernel<false, NA_THREADS, NA_P, NA_MINB, EpiStore>
-        <<<(unsigned)sk.grid, NA_THREADS, 0, st>>>(src, np, src, np, eps2, sk, partials, counters, epi);
+        <<<(unsigned)sk.grid, NA_THREADS, 0, st>>>(src, np, src, np, eps2, sk, partials, counters, epi,
+                                                   nullptr);
   GH_LAUNCH_CHECK();
   return GH_OK;
 }

@@ -216,10 +216,11 @@ int gh_measure_fma_peaks(double* fp32_lane_ops_per_s, double* fp64_lane_ops_per_
 
 /* Measures the pairs per second that the mixed direct sum's pair arithmetic reaches on
  * the current device with every operand in registers (12 FMA-pipe instructions and one
- * MUFU rsqrt per pair, 4 targets per thread, one 512-thread CTA per SM, no memory in
- * the loop): the ceiling of that instruction mix, against which the kernel's pairs per
- * second are compared (no counterpart in the reference). */
-int gh_measure_pair_mix(double* pairs_per_s, void* stream);
+ * MUFU rsqrt per pair; with equal_mass != 0 the loop that systems of equal masses run,
+ * 11 FMA-pipe instructions; 4 targets per thread, one 512-thread CTA per SM, no memory
+ * in the loop): the ceiling of that instruction mix, against which the kernel's pairs
+ * per second are compared (no counterpart in the reference). */
+int gh_measure_pair_mix(int equal_mass, double* pairs_per_s, void* stream);
 
 /* Enables (1) or disables (0) CUDA-event timing of every force-kernel launch (direct
  * FP64, direct mixed, tree walk) on the stream it is launched on (no counterpart in

@@ -79,6 +79,42 @@ def test_mixed_direct_accuracy(lib, cuda, n):
     np.testing.assert_array_equal(got, again)  # deterministic split-tile combine
 
 
+@pytest.mark.parametrize("n", [5000, 65536])
+def test_mixed_equal_mass_loop_matches_general_loop(lib, cuda, n):
+    """A system whose masses are all equal takes the mixed kernel's equal-mass loop
+    (the sum of r^-3 d, the mass applied once per target in FP64); the same system with
+    one mass one ulp larger takes the general loop.  Both agree with the FP64 oracle
+    and with each other to the mixed tolerance, as a force (a packed tile at N = 5000,
+    a scalar one at 65,536) and over one fused leapfrog step."""
+    import torch
+
+    from gravhopper_gb300 import _jbgrav, engine, ics
+    ic = ics.plummer(n, seed=n + 1)
+    m_eq = ic["mass"].copy()
+    m_ne = m_eq.copy()
+    m_ne[n // 2] = np.nextafter(m_ne[n // 2], np.inf)
+    ref = oracle.direct_summation(ic["pos"], m_eq, 5e-5)
+    got_eq = _jbgrav.direct_summation_mixed(ic["pos"], m_eq, 5e-5)
+    got_ne = _jbgrav.direct_summation_mixed(ic["pos"], m_ne, 5e-5)
+    for got in (got_eq, got_ne):
+        rms, mx = rel_err(got, ref)
+        assert rms <= MIXED_RMS_TOL and mx <= MIXED_MAX_TOL, (rms, mx)
+    rms, mx = rel_err(got_eq, got_ne)
+    assert rms <= MIXED_RMS_TOL and mx <= MIXED_MAX_TOL, (rms, mx)
+    assert not np.array_equal(got_eq, got_ne)  # the two loops did run
+    np.testing.assert_array_equal(got_eq, _jbgrav.direct_summation_mixed(ic["pos"], m_eq, 5e-5))
+    states = []
+    for m in (m_eq, m_ne):
+        x = torch.from_numpy(ic["pos"].copy()).to(cuda)
+        v = torch.from_numpy(ic["vel"].copy()).to(cuda)
+        engine.run_dkd(x, v, torch.from_numpy(m).to(cuda), 1, 0.005, 5e-5, precision="mixed")
+        states.append((x.cpu().numpy(), v.cpu().numpy()))
+    # the step's displacement and velocity change (the kick carries the force)
+    for k, start in ((0, ic["pos"]), (1, ic["vel"])):
+        rms, mx = rel_err(states[0][k] - start, states[1][k] - start)
+        assert rms <= MIXED_RMS_TOL and mx <= MIXED_MAX_TOL, (k, rms, mx)
+
+
 def test_mixed_position_and_zero_softening(lib, cuda):
     from gravhopper_gb300 import _jbgrav, ics
     ic = ics.plummer(3000, seed=4)
