@@ -24,6 +24,7 @@ struct EnsSys {
   float eps2;
   double dt;
   double origin[3];
+  double meq;  // the system's common mass when all its masses are equal, else 0
 };
 
 template <bool GUARD, int THREADS, int P>
@@ -61,8 +62,14 @@ __global__ void __launch_bounds__(THREADS)
       hx[p] = hy[p] = hz[p] = lx[p] = ly[p] = lz[p] = 0ull;
     }
     const f2 E2 = f2make(S.eps2, S.eps2);
+    // Equal masses (as direct_mixed_kernel): full chunks sum r^-3 d, staged w is 1
+    // (0 for padding) so the partial last chunk's general loop matches, and each
+    // target's sum is scaled by the mass once.
+    const bool eq = S.meq != 0.0;
+    const double msc = eq ? S.meq : 1.0;
     // Double-buffered source chunks with a register prefetch (see direct_mixed_kernel).
     float4 pre = tid < S.n ? src[S.off + tid] : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (eq) pre.w = tid < S.n ? 1.f : 0.f;
     for (int c0 = 0; c0 < S.n; c0 += JT) {
       float4* tb = tile + buf * (2 * JT);
       tb[2 * tid + 0] = make_float4(pre.x, pre.x, pre.y, pre.y);
@@ -71,8 +78,12 @@ __global__ void __launch_bounds__(THREADS)
       if (c0 + JT < S.n) {
         const int j = c0 + JT + tid;
         pre = j < S.n ? src[S.off + j] : make_float4(0.f, 0.f, 0.f, 0.f);
+        if (eq) pre.w = j < S.n ? 1.f : 0.f;
       }
-      mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      if (eq && c0 + JT <= S.n)
+        mixed_chunk<GUARD, P, JT, true>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
+      else
+        mixed_chunk<GUARD, P, JT>(tb, tx, ty, tz, E2, hx, hy, hz, lx, ly, lz);
       buf ^= 1;
     }
     EpiDKD epi;
@@ -95,9 +106,11 @@ __global__ void __launch_bounds__(THREADS)
       f2split(lz[p], a[5], b[5]);
       const int l0 = t * TILE + (2 * p) * THREADS + tid, l1 = l0 + THREADS;
       if (l0 < S.n)
-        epi(S.off + l0, (double)a[0] + (double)a[1], (double)a[2] + (double)a[3], (double)a[4] + (double)a[5]);
+        epi(S.off + l0, msc * ((double)a[0] + (double)a[1]), msc * ((double)a[2] + (double)a[3]),
+            msc * ((double)a[4] + (double)a[5]));
       if (l1 < S.n)
-        epi(S.off + l1, (double)b[0] + (double)b[1], (double)b[2] + (double)b[3], (double)b[4] + (double)b[5]);
+        epi(S.off + l1, msc * ((double)b[0] + (double)b[1]), msc * ((double)b[2] + (double)b[3]),
+            msc * ((double)b[4] + (double)b[5]));
     }
   }
   if (tid == 0) {
@@ -110,20 +123,26 @@ __global__ void __launch_bounds__(THREADS)
   }
 }
 
-// Mass-weighted centre of each system (one block per system, fixed reduction order).
+// Mass-weighted centre of each system (one block per system, fixed reduction order),
+// and whether all its masses equal its first (finite, nonzero; a NaN never does).
 __global__ void ensemble_origin_kernel(const double* __restrict__ x, const double* __restrict__ mass,
                                        EnsSys* __restrict__ sys) {
   __shared__ dvec4 red[256];
   EnsSys& S = sys[blockIdx.x];
+  const double m0 = S.n > 0 ? mass[S.off] : 0.0;
   dvec4 a = make_dvec4(0.0, 0.0, 0.0, 0.0);
+  bool ne = false;
   for (int k = threadIdx.x; k < S.n; k += 256) {
     const int64_t i = S.off + k;
     const double m = mass[i];
+    ne |= !(m == m0);
     a.x += m * x[3 * i];
     a.y += m * x[3 * i + 1];
     a.z += m * x[3 * i + 2];
     a.w += m;
   }
+  ne = __syncthreads_or(ne);
+  if (threadIdx.x == 0) S.meq = (!ne && m0 != 0.0 && isfinite(m0)) ? m0 : 0.0;
   red[threadIdx.x] = a;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
@@ -215,6 +234,7 @@ int ensemble_run(double* x, double* v, const double* mass, const int64_t* h_off,
     hs[s].eps2 = (float)(h_eps[s] * h_eps[s]);
     hs[s].dt = h_dt[s];
     hs[s].origin[0] = hs[s].origin[1] = hs[s].origin[2] = 0.0;
+    hs[s].meq = 0.0;
     if (!(hs[s].eps2 > 0.f)) guard = true;
     for (int t = 0; t * tile < n; t++) items.push_back(make_int2((int)s, t));
   }
