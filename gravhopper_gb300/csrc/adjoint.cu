@@ -93,15 +93,18 @@ __global__ void __launch_bounds__(AJ_THREADS)
 // register pair, VJ_P packs per thread), sources duplicated per lane pair in shared
 // memory, per-chunk partials folded into two-sum (hi, lo) accumulators; 8 floats of
 // partials per (split, target): hi/lo of gx, gy, gz, gm.  Per pair: 30 FP32 lane-ops
-// (3 sub, 3 fma for s, 4 for q and -3q/s, 6 for u, 3 for d.u, 1, 6 for g, 4 for gm)
-// and one MUFU rsqrt.
+// (3 sub, 3 fma for s, 4 for q and -3q/s, 6 for u (3 with equal masses), 3 for d.u,
+// 1, 6 for g, 4 for gm) and one MUFU rsqrt.
 // ---------------------------------------------------------------------------
 constexpr int VJ_THREADS = 128;
 constexpr int VJ_P = 2;
 constexpr int VJ_TILE = VJ_THREADS * 2 * VJ_P;
 constexpr int VJ_JT = VJ_THREADS;
 
-template <bool SELFCHK>
+// EQ (all masses equal): u = m (lambda_j - lambda_k) with the mass taken out, one
+// subtraction instead of a product and an FMA per component; the caller scales the
+// position gradient by m once (the mass gradient's terms hold no mass).
+template <bool SELFCHK, bool EQ = false>
 __device__ __forceinline__ void vjp_chunk(const float4* __restrict__ tile, int64_t jbase, const int64_t* ka,
                                           const f2* tx, const f2* ty, const f2* tz, const f2* tm, const f2* tlx,
                                           const f2* tly, const f2* tlz, f2 E2, f2* gx, f2* gy, f2* gz, f2* gm) {
@@ -128,9 +131,9 @@ __device__ __forceinline__ void vjp_chunk(const float4* __restrict__ tile, int64
       const f2 r2 = f2mul(r, r);
       const f2 q = f2mul(r2, r);
       const f2 np = f2mul(f2mul(q, M3), r2);
-      const f2 ux = f2fma(NM, tlx[p], f2mul(tm[p], LX));
-      const f2 uy = f2fma(NM, tly[p], f2mul(tm[p], LY));
-      const f2 uz = f2fma(NM, tlz[p], f2mul(tm[p], LZ));
+      const f2 ux = EQ ? f2sub(LX, tlx[p]) : f2fma(NM, tlx[p], f2mul(tm[p], LX));
+      const f2 uy = EQ ? f2sub(LY, tly[p]) : f2fma(NM, tly[p], f2mul(tm[p], LY));
+      const f2 uz = EQ ? f2sub(LZ, tlz[p]) : f2fma(NM, tlz[p], f2mul(tm[p], LZ));
       f2 du = f2mul(dx, ux);
       du = f2fma(dy, uy, du);
       du = f2fma(dz, uz, du);
@@ -148,12 +151,16 @@ __device__ __forceinline__ void vjp_chunk(const float4* __restrict__ tile, int64
 
 __global__ void __launch_bounds__(VJ_THREADS, 4)
     vjp_mixed_kernel(const float4* __restrict__ src, const float4* __restrict__ lsrc, int64_t n, float eps2,
-                     int64_t jlen, float* __restrict__ part) {
+                     int64_t jlen, float* __restrict__ part, const double* __restrict__ meqp) {
   __shared__ __align__(16) float4 tile[4 * VJ_JT];
   const int tid = threadIdx.x;
   const int64_t tbase = (int64_t)blockIdx.x * VJ_TILE;
   const int64_t split = blockIdx.y;
   const int64_t j0 = split * jlen, j1 = (j0 + jlen) < n ? j0 + jlen : n;
+  // equal masses: the sums are taken with unit masses (staged as such for the general
+  // loop of a partial chunk: -1 for a source, 0 for padding, 1 for every target) and the
+  // position gradient is scaled by the mass in the reduction
+  const bool eq = __ldg(meqp) != 0.0;
   f2 tx[VJ_P], ty[VJ_P], tz[VJ_P], tm[VJ_P], tlx[VJ_P], tly[VJ_P], tlz[VJ_P];
   f2 hx[VJ_P], hy[VJ_P], hz[VJ_P], hm[VJ_P], lx[VJ_P], ly[VJ_P], lz[VJ_P], lm[VJ_P];
   int64_t ka[2 * VJ_P];
@@ -170,7 +177,7 @@ __global__ void __launch_bounds__(VJ_THREADS, 4)
     tx[p] = f2make(P0[0].x, P0[1].x);
     ty[p] = f2make(P0[0].y, P0[1].y);
     tz[p] = f2make(P0[0].z, P0[1].z);
-    tm[p] = f2make(P0[0].w, P0[1].w);
+    tm[p] = eq ? f2make(1.f, 1.f) : f2make(P0[0].w, P0[1].w);
     tlx[p] = f2make(L0[0].x, L0[1].x);
     tly[p] = f2make(L0[0].y, L0[1].y);
     tlz[p] = f2make(L0[0].z, L0[1].z);
@@ -183,8 +190,9 @@ __global__ void __launch_bounds__(VJ_THREADS, 4)
       const int64_t j = c + tid;
       const float4 P = j < j1 ? src[j] : make_float4(0.f, 0.f, 0.f, 0.f);
       const float4 L = j < j1 ? lsrc[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float w = eq ? (j < j1 ? 1.f : 0.f) : P.w;
       tile[4 * tid + 0] = make_float4(P.x, P.x, P.y, P.y);
-      tile[4 * tid + 1] = make_float4(P.z, P.z, -P.w, -P.w);
+      tile[4 * tid + 1] = make_float4(P.z, P.z, -w, -w);
       tile[4 * tid + 2] = make_float4(L.x, L.x, L.y, L.y);
       tile[4 * tid + 3] = make_float4(L.z, L.z, 0.f, 0.f);
     }
@@ -193,10 +201,18 @@ __global__ void __launch_bounds__(VJ_THREADS, 4)
 #pragma unroll
     for (int p = 0; p < VJ_P; p++) gx[p] = gy[p] = gz[p] = gm[p] = 0ull;
     // only a chunk that overlaps this tile's targets can pair a target with itself
-    if (c < tbase + VJ_TILE && c + VJ_JT > tbase)
-      vjp_chunk<true>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
-    else
-      vjp_chunk<false>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+    const bool self = c < tbase + VJ_TILE && c + VJ_JT > tbase;
+    if (eq && c + VJ_JT <= j1) {  // a full chunk of equal masses
+      if (self)
+        vjp_chunk<true, true>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+      else
+        vjp_chunk<false, true>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+    } else {
+      if (self)
+        vjp_chunk<true>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+      else
+        vjp_chunk<false>(tile, c, ka, tx, ty, tz, tm, tlx, tly, tlz, E2, gx, gy, gz, gm);
+    }
 #pragma unroll
     for (int p = 0; p < VJ_P; p++) {
       f2 sm, e;
@@ -258,7 +274,8 @@ __global__ void vjp_reduce_f64_kernel(const double* __restrict__ part, int split
 }
 
 __global__ void vjp_reduce_mixed_kernel(const float* __restrict__ part, int splits, int64_t n,
-                                        double* __restrict__ gpos, double* __restrict__ gmass) {
+                                        const double* __restrict__ meqp, double* __restrict__ gpos,
+                                        double* __restrict__ gmass) {
   const int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= n) return;
   double a[4] = {0.0, 0.0, 0.0, 0.0};
@@ -267,9 +284,11 @@ __global__ void vjp_reduce_mixed_kernel(const float* __restrict__ part, int spli
       const float* o = part + ((int64_t)s * n + k) * 8;
       a[q] += (double)o[2 * q] + (double)o[2 * q + 1];
     }
-  gpos[3 * k] = a[0];
-  gpos[3 * k + 1] = a[1];
-  gpos[3 * k + 2] = a[2];
+  const double meq = *meqp;
+  const double sm = meq != 0.0 ? meq : 1.0;  // equal masses: the sums were taken with unit masses
+  gpos[3 * k] = sm * a[0];
+  gpos[3 * k + 1] = sm * a[1];
+  gpos[3 * k + 2] = sm * a[2];
   if (gmass) gmass[k] = a[3];
 }
 
@@ -328,17 +347,24 @@ __global__ void vjp_prepare_mixed_kernel(const double* __restrict__ pos, const d
   lsrc[i] = make_float4((float)lam[3 * i], (float)lam[3 * i + 1], (float)lam[3 * i + 2], 0.f);
 }
 
+// origin[0..2]: the mass-weighted centre; origin[3]: the common mass when every mass
+// equals the first (finite, nonzero; a NaN never does), else 0.
 __global__ void mean_origin_kernel(const double* __restrict__ pos, const double* __restrict__ mass, int64_t n,
                                    double* __restrict__ origin) {
   __shared__ dvec4 red[256];
+  const double m0 = n > 0 ? mass[0] : 0.0;
   dvec4 a = make_dvec4(0.0, 0.0, 0.0, 0.0);
+  bool ne = false;
   for (int64_t i = threadIdx.x; i < n; i += 256) {
     const double m = mass[i];
+    ne |= !(m == m0);
     a.x += m * pos[3 * i];
     a.y += m * pos[3 * i + 1];
     a.z += m * pos[3 * i + 2];
     a.w += m;
   }
+  ne = __syncthreads_or(ne);
+  if (threadIdx.x == 0) origin[3] = (!ne && m0 != 0.0 && isfinite(m0)) ? m0 : 0.0;
   red[threadIdx.x] = a;
   __syncthreads();
   for (int s = 128; s > 0; s >>= 1) {
@@ -422,10 +448,12 @@ int direct_vjp(const double* pos, const double* mass, int64_t n, double eps, con
   GH_TRY(ensure(ws.part, (size_t)msplits * n * 8 * sizeof(float)));
   prof_begin(st);
   vjp_mixed_kernel<<<dim3((unsigned)mtiles, (unsigned)msplits), VJ_THREADS, 0, st>>>(
-      (const float4*)ws.src.ptr, (const float4*)ws.lsrc.ptr, n, (float)(eps * eps), mjlen, (float*)ws.part.ptr);
+      (const float4*)ws.src.ptr, (const float4*)ws.lsrc.ptr, n, (float)(eps * eps), mjlen, (float*)ws.part.ptr,
+      (const double*)ws.origin.ptr + 3);
   prof_end(st);
   GH_LAUNCH_CHECK();
-  vjp_reduce_mixed_kernel<<<rb, 256, 0, st>>>((const float*)ws.part.ptr, (int)msplits, n, gpos, gmass);
+  vjp_reduce_mixed_kernel<<<rb, 256, 0, st>>>((const float*)ws.part.ptr, (int)msplits, n,
+                                              (const double*)ws.origin.ptr + 3, gpos, gmass);
   GH_LAUNCH_CHECK();
   return GH_OK;
 }

@@ -35,12 +35,17 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+@pytest.mark.parametrize("equal_masses", [True, False])
 @pytest.mark.parametrize("precision,tol", [("fp64", 1e-11), ("mixed", 1e-5)])
-def test_vjp_against_dense_autograd(lib, cuda, precision, tol):
+def test_vjp_against_dense_autograd(lib, cuda, precision, tol, equal_masses):
+    """Equal masses (the Plummer sphere's) run the mixed kernel's equal-mass loop, the
+    mass applied to the position gradient once; unequal ones the general loop."""
     import torch
 
     from gravhopper_gb300 import engine, ics
     ic = ics.plummer(700, seed=2)
+    if not equal_masses:
+        ic["mass"] = ic["mass"] * np.random.default_rng(5).uniform(0.5, 1.5, size=700)
     x = torch.from_numpy(ic["pos"]).to(cuda)
     m = torch.from_numpy(ic["mass"]).to(cuda)
     lam = torch.randn((700, 3), dtype=torch.float64, device=cuda, generator=torch.Generator(cuda).manual_seed(0))
