@@ -35,6 +35,20 @@ def _load_cache(path):
         return {}
 
 
+def save_cache(path, cache):
+    """Writes the tuning cache: a private file renamed over ``path``, so that ranks of
+    one job tuning at the same time never leave a torn file behind (a reader sees the
+    old cache or a whole new one).  A cache that cannot be written is skipped."""
+    try:
+        os.makedirs(os.path.dirname(path), exist_ok=True)
+        tmp = f"{path}.{os.getpid()}.tmp"
+        with open(tmp, "w") as f:
+            json.dump(cache, f, indent=1)
+        os.replace(tmp, path)
+    except OSError:
+        pass
+
+
 def _time_shape(call, shape, reps):
     _capi.call("gh_direct_set_shape", shape)
     try:
@@ -114,12 +128,7 @@ def tune_direct(sizes=(2048, 8192, 24576, 65536, 262144, 1048576), kinds=("force
             n_min = n // 2 if k == 0 else int(math.sqrt(sizes[k - 1] * n)) + 1
             _capi.call("gh_direct_tune", n_min, fused, out[kind][n][0])
     if use_cache and dirty:
-        try:
-            os.makedirs(os.path.dirname(path), exist_ok=True)
-            with open(path, "w") as f:
-                json.dump(cache, f, indent=1)
-        except OSError:
-            pass
+        save_cache(path, cache)
     return out
 
 

@@ -102,12 +102,8 @@ def autotune(ens: Ensemble, steps=4, use_cache=True):
     ens.config = best
     if use_cache:
         cache[key] = {"best": best, "ms": times, "when": time.time()}
-        try:
-            os.makedirs(os.path.dirname(path), exist_ok=True)
-            with open(path, "w") as f:
-                json.dump(cache, f, indent=1)
-        except OSError:
-            pass
+        from .autotune import save_cache
+        save_cache(path, cache)
     return best, times
 
 
