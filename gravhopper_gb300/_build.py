@@ -7,6 +7,7 @@ is skipped when the library is newer than every source and header.
 """
 from __future__ import annotations
 
+import fcntl
 import glob
 import os
 import subprocess
@@ -46,10 +47,26 @@ def up_to_date() -> bool:
     return all(os.path.getmtime(p) <= t for p in _deps())
 
 
+LOCK = os.path.join(PKG, ".build.lock")
+
+
 def build(force: bool = False, verbose: bool = False, ptxas_info: bool = False) -> str:
-    """Compile and link the library; returns its path."""
+    """Compile and link the library; returns its path.  Processes that build at the same
+    time (the ranks of one job) take turns on an exclusive lock file, and a process that
+    gets the lock after another has built finds the library up to date."""
     if not force and not ptxas_info and up_to_date():
         return LIB
+    with open(LOCK, "a") as lock:
+        fcntl.flock(lock, fcntl.LOCK_EX)
+        try:
+            if not force and not ptxas_info and up_to_date():
+                return LIB
+            return _build_locked(verbose, ptxas_info)
+        finally:
+            fcntl.flock(lock, fcntl.LOCK_UN)
+
+
+def _build_locked(verbose: bool, ptxas_info: bool) -> str:
     os.makedirs(OBJ, exist_ok=True)
     nvcc = _nvcc()
     extra = ["-Xptxas", "-v"] if ptxas_info else []
