@@ -35,15 +35,18 @@ HISTORY_SEGMENT_BYTES = 256 << 20
 
 
 class GravHopperException(Exception):
-    """Parent class for all error exceptions."""
+    """Base of the errors this module raises (the reference's class names, so that
+    callers' except clauses keep working)."""
 
 
 class UninitializedSimulationException(GravHopperException):
-    """Exception for trying to run a simulation without any initial conditions."""
+    """run() or a snapshot accessor was called before any particles were added."""
 
 
 class ICException(GravHopperException):
-    """Exception for trying to add ICs that don't make sense."""
+    """Initial conditions are malformed (a key missing, lengths that disagree, an IC
+    generator called without its parameters); the message is also printed, as the
+    reference does."""
 
     def __init__(self, msg):
         super().__init__(msg)
@@ -51,11 +54,12 @@ class ICException(GravHopperException):
 
 
 class UnknownAlgorithmException(GravHopperException):
-    """Exception for using an unknown N-body algorithm name."""
+    """The force algorithm is neither 'tree' nor 'direct'."""
 
 
 class ExternalPackageException(GravHopperException):
-    """Exception for calling a pynbody/galpy/gala/agama function when not using them."""
+    """A feature that needs galpy, gala, agama or pynbody was called; those packages
+    are not part of this engine.  The message is also printed."""
 
     def __init__(self, msg):
         super().__init__(msg)
