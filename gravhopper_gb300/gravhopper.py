@@ -376,7 +376,8 @@ class Simulation(object):
             torch.from_numpy(self._vel[first:first + k]).copy_(hv)
 
     def init_run(self, Nsnap=None):
-        """Initialise an N-body run (gravhopper.py:324-342)."""
+        """Allocates the (Nsnap, Np, 3) position and velocity histories and puts the ICs in
+        slot 0 (gravhopper.py:324-342)."""
         if self.ICarrays is False:
             raise UninitializedSimulationException
         self.Nsnap = Nsnap + 1
@@ -391,7 +392,7 @@ class Simulation(object):
         self.running = True
 
     def reset(self):
-        """Back to the state before init_run(); ICs and external forces are kept."""
+        """Drops the run's histories and times; the ICs and registered external forces stay."""
         self.running = False
         self._pos = self._vel = self._mass = self._times = None
         self.Nsnap = 0
