@@ -239,10 +239,14 @@ def main():
 
     tuned = None
     if args.precision == "mixed" and not shard:
-        # the tile shape of this size's fused step, picked by timing every shape (untimed here)
+        # the tile shapes of this size's fused step (the timed step) and force (the
+        # end-to-end call), picked by timing every shape (untimed here)
         from gravhopper_gb300 import autotune
-        best, ms = autotune.tune_direct(sizes=(n,), kinds=("step",), device=dev)["step"][n]
-        tuned = {"shape": best, "ms_per_step_by_shape": {k: round(t, 2) for k, t in ms.items()}}
+        res = autotune.tune_direct(sizes=(n,), kinds=("step", "force"), device=dev)
+        best, ms = res["step"][n]
+        fbest, fms = res["force"][n]
+        tuned = {"shape": best, "ms_per_step_by_shape": {k: round(t, 2) for k, t in ms.items()},
+                 "force_shape": fbest, "ms_per_force_by_shape": {k: round(t, 2) for k, t in fms.items()}}
 
     for _ in range(args.warmup):
         step()
@@ -261,9 +265,6 @@ def main():
         barrier()
     launches = _capi.launch_count() - launches0
     _capi.kernel_timing(False)
-    if tuned is not None:
-        from gravhopper_gb300 import autotune
-        autotune.clear_direct()  # the other measurements use the library's own size table
     kern_ms, kern_n = _capi.kernel_timing_collect()
     step_ms = sum(a.elapsed_time(b) for a, b in ev)
     t = torch.tensor([step_ms], dtype=torch.float64, device=dev)
@@ -290,6 +291,9 @@ def main():
         e2e_s += time.perf_counter() - t0
     e2e = {"value": world * pairs * e2e_steps / e2e_s / 1e9, "unit": UNIT,
            "h2d_bytes_per_step": n * 3 * 8 + n * 8, "d2h_bytes_per_step": n * 3 * 8}
+    if tuned is not None:
+        from gravhopper_gb300 import autotune
+        autotune.clear_direct()  # the other measurements use the library's own size table
 
     kern_avg_s = kern_ms / max(kern_n, 1) * 1e-3
     # pairs one force launch evaluates (sharded: this rank's targets, own and others' sources)
