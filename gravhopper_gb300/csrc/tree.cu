@@ -750,6 +750,7 @@ constexpr int TW_FOLD = 32;
 // instructions; each lane still adds its interactions in visiting order.
 constexpr int TW_FQ = 32;
 constexpr int TW_FQ_ROUND = 28;
+static_assert((TW_FQ & (TW_FQ - 1)) == 0, "the FIFO index wraps with a mask");
 
 // One FP64 interaction: the cell's monopole (nM) with s^(-3/2) on the integer pipes,
 // FP64 Newton steps outside the emulation's range.
