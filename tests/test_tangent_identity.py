@@ -28,3 +28,13 @@ def test_jvp_equals_mass_weighted_vjp(eps):
     (vjp,) = vjp_fn(m[:, None] * u)
     assert torch.isfinite(jvp).all()
     np.testing.assert_allclose((vjp / m[:, None]).numpy(), jvp.numpy(), rtol=1e-12, atol=1e-12 * float(jvp.abs().max()))
+
+
+def test_tangent_rollout_refuses_zero_mass():
+    """The identity divides by the masses: a zero mass is refused before any work."""
+    torch = pytest.importorskip("torch")
+    from gravhopper_gb300.adjoint import tangent_rollout
+    x = torch.zeros((4, 3), dtype=torch.float64)
+    m = torch.tensor([1.0, 0.0, 1.0, 1.0], dtype=torch.float64)
+    with pytest.raises(ValueError, match="nonzero"):
+        tangent_rollout(x, x, m, 1, 0.005, 5e-5, x)
